@@ -1,0 +1,384 @@
+#!/usr/bin/env python3
+"""Benchmark of the 3D pure-qP VTI forward modeling loop on GB300.
+
+Workload (one bench "step" = one whole shot): layered VTI model 400x400x300
+cells + 30-cell PML (460x460x360 padded, 76.2 M cells), 10 m spacing, 3000
+time steps of 0.5 ms, 20 Hz Ricker source at the surface centre, receivers on
+the full surface, xz/yz wavefield slices every 100 steps.  Synthetic, seeded
+(no field data is available); the working set (~4.8 GB) is far larger than
+the 129 MB L2, so no flush is needed between steps.
+
+Metric: Gcell-updates/s = padded cells x time steps / seconds.
+  value      device time (CUDA events on the library's stream) of K shots with
+             the model resident in HBM: reset + 3000 steps + slice snapshots
+  e2e        the same shots through qp3d_forward (the modeling3d replacement)
+             from pinned host buffers: model upload, time loop, record download
+  roofline   the fused step kernel: algorithmic bytes per launch
+             (24 B per interior cell + 64 B per PML cell) / its mean duration,
+             against the measured HBM copy bandwidth
+  cpu_baseline  the reference CPU arithmetic (oracle port of CPU_function.c,
+             bit-exact to it) on all host cores, on a bounded sample
+
+--impl reference runs only that CPU implementation, a few time steps of the
+same workload per bench step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gpu-c_3dqmodeling_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(hx=400, hy=400, nz0=300, pml=30, nt=3000, dt=5e-4, dx=10.0, fm=20.0,
+                seed=2, snap_every=100)
+WORKLOAD_NAME = ("layered VTI 400x400x300 + 30-cell PML (460x460x360 padded), 12 dipping "
+                 "layers seed 2, 3000 steps x 0.5 ms, 20 Hz Ricker at surface centre, "
+                 "full-surface receivers, xz/yz slices every 100 steps")
+REF_SAMPLE_STEPS = 2      # time steps per reference-arm bench step
+CPU_SAMPLE_STEPS = 6      # time steps of the in-line CPU baseline
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="qp3d", choices=["qp3d", "reference"])
+    ap.add_argument("--nt", type=int, default=None, help="override time steps (testing)")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="scale the horizontal/vertical extent (testing only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    w = dict(WORKLOAD)
+    if args.nt is not None:
+        w["nt"] = args.nt
+    if args.scale != 1.0:
+        for k in ("hx", "hy", "nz0"):
+            w[k] = max(16, int(round(w[k] * args.scale)))
+    return w
+
+
+def make_shot(w):
+    import synthetic
+    return synthetic.layered_vti(hx=w["hx"], hy=w["hy"], nz0=w["nz0"], pml=w["pml"],
+                                 nt=w["nt"], dx=w["dx"], dt=w["dt"], fm=w["fm"],
+                                 seed=w["seed"])
+
+
+def algorithmic_bytes(shot):
+    """24 B per interior cell (read u(k), u(k-1), vp, eps, delta; write u(k+1))
+    + 64 B per PML cell (u(k), vp, eps, delta, 7 state reads, 4 state writes,
+    u(k+1)), over the updated box as the reference defines the layers."""
+    n = shot.N
+    ni = (shot.nx - 2 * shot.pml) * (shot.ny - 2 * shot.pml) * (shot.nz - 2 * shot.pml)
+    return 24 * ni + 64 * (n - ni), ni, n - ni
+
+
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = "nccl" if os.environ.get("QP3D_BENCH_BACKEND", "gloo") == "nccl" else "gloo"
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu_index):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+            except ValueError:
+                continue
+            for name, flag in zip(self.NAMES, r[3:]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per cell of one step-kernel launch from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["qp3d_step_kernel"]["dram_bytes_per_cell"]), d["qp3d_step_kernel"].get("case")
+    except Exception:
+        return None, None
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(shot, nsteps, k0=1500, seed=0):
+    """Reference CPU arithmetic (oracle REF32 port, all host threads) for
+    nsteps from a dense random state; returns (seconds, threads)."""
+    from oracle import oracle as O
+    import synthetic
+    prob = shot.to_oracle(O)
+    u_prev, u_cur, pml = synthetic.random_state(shot, seed=seed)
+    st = O.State(prob)
+    st.u1[:] = u_prev
+    st.u2[:] = u_cur
+    st.pml[:] = pml
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.run(O.REF32, prob, k0=k0, nsteps=nsteps, state=st, nthreads=threads, want_record=False)
+    return time.perf_counter() - t0, threads
+
+
+def run_reference_arm(args, dist):
+    if dist.rank != 0:
+        return 0
+    w = workload(args)
+    shot = make_shot(w)
+    cells = shot.N
+    times = []
+    threads = os.cpu_count() or 1
+    for i in range(args.warmup + args.steps):
+        dt, threads = cpu_sample(shot, REF_SAMPLE_STEPS, k0=1500 + i, seed=i)
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = cells * REF_SAMPLE_STEPS * args.steps / total / 1e9
+    sample = ("%d time steps of the %dx%dx%d padded grid per bench step, from a dense random "
+              "state, oracle port of CPU_function.c (bit-exact to it), OpenMP %d threads" %
+              (REF_SAMPLE_STEPS, shot.nx, shot.ny, shot.nz, threads))
+    line = {
+        "impl": "reference", "metric": "Gcell-updates/s", "value": round(value, 6),
+        "unit": "Gcell/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "step": "bounded sample: %d time steps" %
+                   REF_SAMPLE_STEPS, "cells": cells, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gcell/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_gpu_arm(args, dist):
+    import qp3d
+    w = workload(args)
+    shot = make_shot(w)
+    nt = shot.nt
+    cells = shot.N
+    dev = dist.local
+    ctx = qp3d.Context(dev)
+    snap = qp3d.make_snap(lambda step, kind, arr: 0, w["snap_every"], [qp3d.SNAP_XZ, qp3d.SNAP_YZ])
+    every = w["snap_every"]
+    snaps_per_shot = len(range(0, nt, every))
+
+    def one_shot(per_kernel):
+        """reset + nt steps + slices; returns (ms_step_kernel, ms_gradmax) sums."""
+        ctx.reset()
+        k, ms_s, ms_g = 0, 0.0, 0.0
+        while k < nt:
+            nxt = k if k % every == 0 else (k // every + 1) * every
+            n = min(nt - k, nxt - k + 1)
+            if per_kernel:
+                _, a, b = ctx.time(n, per_kernel=True)
+                ms_s += a
+                ms_g += b
+            else:
+                ctx.advance(n)
+            k += n
+            if (k - 1) % every == 0:
+                ctx.snapshot(snap)
+        return ms_s, ms_g
+
+    ctx.load(shot)
+    for _ in range(args.warmup):
+        one_shot(False)
+    ctx.sync()
+    dist.barrier()
+    gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dev]
+                 if os.environ.get("CUDA_VISIBLE_DEVICES") else dev)
+    clocks = Clocks(gpu_index)
+    ctx.event(0)
+    ms_step, ms_grad = 0.0, 0.0
+    for _ in range(args.steps):
+        a, b = one_shot(True)
+        ms_step += a
+        ms_grad += b
+    ctx.event(1)
+    ctx.sync()
+    ms = ctx.elapsed(0, 1)
+    clk = clocks.stop()
+    dist.barrier()
+    ms = dist.max(ms)
+    value = dist.world * cells * nt * args.steps / (ms / 1e3) / 1e9
+    launches_per_step = ctx.launches_per_step()
+    gpu_launches = (launches_per_step * nt + 2 * snaps_per_shot) * args.steps
+
+    # roofline of the fused step kernel (one launch = one time step)
+    bstep, ni, np_ = algorithmic_bytes(shot)
+    n_launch = nt * args.steps
+    t_step = ms_step / n_launch / 1e3
+    achieved = bstep / t_step / 1e9
+    peak, peak_kind = hbm_peak()
+    tpc, tcase = traffic_per_cell()
+    roofline = {"bound": "hbm", "kernel": "qp3d_step_kernel", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_kind": peak_kind + " copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": bstep,
+                "traffic": (round(tpc * cells) if tpc else None),
+                "traffic_note": ("ncu dram read+write of one launch on %s, scaled per cell" % tcase)
+                if tpc else "no ncu capture committed",
+                "step_kernel_ms": round(ms_step / n_launch, 5),
+                "gradmax_kernel_ms": round(ms_grad / n_launch, 5),
+                "gradmax_read_bytes": 4 * cells}
+
+    # end to end through the C ABI from pinned host memory
+    pin = {}
+    for key in ("vp", "eps", "delta", "src", "wavelet"):
+        a = getattr(shot, key)
+        pa = qp3d.PinnedArray(a.shape)
+        pa.array[:] = a
+        pin[key] = pa
+    rec = qp3d.PinnedArray((nt, shot.hx, shot.hy))
+    pshot = qp3d.Shot(shot.nx, shot.ny, shot.nz, shot.pml, shot.sz, shot.dx, shot.dy, shot.dz,
+                      shot.dt, pin["vp"].array, pin["eps"].array, pin["delta"].array,
+                      pin["src"].array, pin["wavelet"].array, shot.prof, shot.c, shot.c2)
+    ctx.forward(pshot, snap=snap, record=rec.array)     # warm-up
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.forward(pshot, snap=snap, record=rec.array)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = dist.world * cells * nt * args.steps / e2e_s / 1e9
+    h2d = 3 * cells * 4 + nt * 4 + 6 * shot.pml * 4 + 2 * 36 * 4
+    d2h = nt * shot.hx * shot.hy * 4 + snaps_per_shot * (shot.nz - 2 * shot.pml) * (shot.hx + shot.hy) * 4
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        secs, threads = cpu_sample(shot, CPU_SAMPLE_STEPS)
+        cpu = {"value": round(cells * CPU_SAMPLE_STEPS / secs / 1e9, 6), "unit": "Gcell/s",
+               "cores": threads, "kind": "port",
+               "sample": "%d time steps of this grid from a dense random state; oracle port of "
+                         "CPU_function.c (bit-exact to it), OpenMP" % CPU_SAMPLE_STEPS}
+
+    if dist.rank == 0:
+        line = {
+            "metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "step": "one shot of %d time steps" % nt,
+                       "grid": [shot.nx, shot.ny, shot.nz], "cells": cells,
+                       "interior_cells": ni, "pml_cells": np_, "nt": nt,
+                       "l2": "inputs larger than L2 (working set %.1f GB)" %
+                             (15 * cells * 4 / 1e9),
+                       "parallelism": "replicas" if dist.world > 1 else "single"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(1000 * e2e_s / args.steps, 2)},
+            "gpu_launches": gpu_launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    for p in list(pin.values()) + [rec]:
+        p.free()
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference_arm(args, dist)
+        return run_gpu_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

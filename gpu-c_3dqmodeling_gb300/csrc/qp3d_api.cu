@@ -1,0 +1,779 @@
+// qp3d_api.cu -- the C ABI of include/qp3d.h: context, shot buffers, the
+// per-step launch sequence and state I/O.
+//
+// The reference's per-shot driver (3dPureqPModeling_single_shot.cu:26-447)
+// allocates 70 device buffers per call, copies three full volumes to the host
+// every step to find max|grad u| on one CPU core, and copies the whole
+// wavefield back every step to take one receiver plane.  Here the model stays
+// resident, the maximum is a device reduction, the receiver plane is written
+// by the step kernel, and nothing crosses the host link inside the time loop
+// except optional snapshots.
+#include "qp3d_internal.h"
+#include "../../include/qp3d.h"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace qp3d {
+// qp3d_host.cpp: host derivations shared with the drop-in driver.
+void derive_coefs(const float *c, const float *c2, float dx, float dy, float dz, Coefs *k);
+void derive_layers(const float *d, const float *dd, int pml, float dt, float4 *out);
+}  // namespace qp3d
+
+using namespace qp3d;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+struct qp3d_ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    EncodeTiledFn encode = nullptr;
+    char err[512] = {0};
+
+    // shot
+    bool loaded = false;
+    qp3d_geom g{};
+    int ldy = 0;
+    long long plane = 0, vol = 0;
+    int hx = 0, hy = 0;
+    int tile_x = 0, nxt = 0, nyt = 0, nchunks = 0, chunk_z = 0;
+    size_t smem = 0;
+    bool rec_fused = true;
+    float *U[2] = {nullptr, nullptr};
+    float *K = nullptr, *E2 = nullptr, *R8 = nullptr;
+    float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21 = nullptr;
+    float *record = nullptr;
+    float *gmax = nullptr;
+    float4 *layers = nullptr;
+    SrcEntry *src_fused = nullptr, *src_band = nullptr, *src_all = nullptr;
+    int n_fused = 0, n_band = 0, n_all = 0;
+    bool fuse_sources = true;
+    unsigned *errword = nullptr;
+    CUtensorMap tm[2];
+    Coefs coefs{};
+    std::vector<float> wavelet;
+    int step = 0;
+    int cur = 0;           // U[cur] holds u(step)
+    // snapshot staging
+    float *snap_dev = nullptr;
+    float *snap_host = nullptr;
+    size_t snap_cap = 0;
+    cudaEvent_t ev[4] = {};
+    cudaEvent_t uev[8] = {};
+};
+
+// ---------------------------------------------------------------------------
+static int fail(qp3d_ctx *c, int code, const char *fmt, ...)
+{
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c->err, sizeof(c->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define CK(call)                                                                           \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? QP3D_ERR_NOMEM : QP3D_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+extern "C" int qp3d_version(void) { return 10000; }
+
+extern "C" const char *qp3d_strerror(int code)
+{
+    switch (code) {
+    case QP3D_OK: return "ok";
+    case QP3D_ERR_ARG: return "invalid argument";
+    case QP3D_ERR_CUDA: return "CUDA error";
+    case QP3D_ERR_NOMEM: return "out of memory";
+    case QP3D_ERR_TIMEOUT: return "device wait timed out";
+    case QP3D_ERR_STATE: return "invalid call order";
+    case QP3D_ERR_IO: return "file I/O error";
+    case QP3D_ERR_CALLBACK: return "snapshot callback failed";
+    default: return "unknown error";
+    }
+}
+
+extern "C" const char *qp3d_ctx_last_error(const qp3d_ctx *ctx) { return ctx ? ctx->err : ""; }
+
+static void free_shot(qp3d_ctx *ctx)
+{
+    cudaSetDevice(ctx->device);
+    float **bufs[] = {&ctx->U[0], &ctx->U[1], &ctx->K,     &ctx->E2,    &ctx->R8,
+                      &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0], &ctx->W3[1],
+                      &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],  &ctx->W21,
+                      &ctx->record, &ctx->gmax, &ctx->snap_dev};
+    for (float **b : bufs) {
+        if (*b) cudaFree(*b);
+        *b = nullptr;
+    }
+    if (ctx->layers) cudaFree(ctx->layers);
+    if (ctx->src_fused) cudaFree(ctx->src_fused);
+    if (ctx->src_band) cudaFree(ctx->src_band);
+    if (ctx->src_all) cudaFree(ctx->src_all);
+    if (ctx->snap_host) cudaFreeHost(ctx->snap_host);
+    ctx->layers = nullptr;
+    ctx->src_fused = ctx->src_band = ctx->src_all = nullptr;
+    ctx->snap_host = nullptr;
+    ctx->snap_cap = 0;
+    ctx->loaded = false;
+}
+
+extern "C" int qp3d_ctx_create(int device, qp3d_ctx **out)
+{
+    if (!out) return QP3D_ERR_ARG;
+    *out = nullptr;
+    qp3d_ctx *ctx = new (std::nothrow) qp3d_ctx();
+    if (!ctx) return QP3D_ERR_NOMEM;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= 0 || device < 0 || device >= ndev) {
+        delete ctx;
+        return QP3D_ERR_CUDA;
+    }
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        configure_kernels() != cudaSuccess) {
+        delete ctx;
+        return QP3D_ERR_CUDA;
+    }
+    for (auto &ev : ctx->ev) cudaEventCreate(&ev);
+    for (auto &ev : ctx->uev) cudaEventCreate(&ev);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        qp3d_ctx_destroy(ctx);
+        return QP3D_ERR_CUDA;
+    }
+    ctx->encode = reinterpret_cast<EncodeTiledFn>(fn);
+    *out = ctx;
+    return QP3D_OK;
+}
+
+extern "C" void qp3d_ctx_destroy(qp3d_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_shot(ctx);
+    if (ctx->errword) cudaFree(ctx->errword);
+    for (auto &ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto &ev : ctx->uev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+// ---------------------------------------------------------------------------
+static int check_geom(qp3d_ctx *ctx, const qp3d_geom *g)
+{
+    if (!g) return fail(ctx, QP3D_ERR_ARG, "null geometry");
+    if (g->nx < 11 || g->ny < 11 || g->nz < 11)
+        return fail(ctx, QP3D_ERR_ARG, "grid %dx%dx%d smaller than 11 cells", g->nx, g->ny, g->nz);
+    if (g->pml < 0 || g->pml > kMaxPml || 2 * g->pml >= g->nx || 2 * g->pml >= g->ny ||
+        2 * g->pml >= g->nz)
+        return fail(ctx, QP3D_ERR_ARG, "pml %d invalid for grid %dx%dx%d", g->pml, g->nx, g->ny,
+                    g->nz);
+    if (g->nt < 0) return fail(ctx, QP3D_ERR_ARG, "nt < 0");
+    if (g->sz < 0 || g->sz >= g->nz) return fail(ctx, QP3D_ERR_ARG, "sz %d outside [0,%d)", g->sz, g->nz);
+    if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->dt > 0))
+        return fail(ctx, QP3D_ERR_ARG, "non-positive spacing or time step");
+    long long n = (long long)g->nx * g->ny * g->nz;
+    if (n > (1ll << 40)) return fail(ctx, QP3D_ERR_ARG, "grid too large");
+    return QP3D_OK;
+}
+
+static int make_tmap(qp3d_ctx *ctx, float *base, CUtensorMap *tm)
+{
+    const qp3d_geom &g = ctx->g;
+    cuuint64_t dims[3] = {(cuuint64_t)g.ny, (cuuint64_t)g.nx, (cuuint64_t)g.nz};
+    cuuint64_t strides[2] = {(cuuint64_t)ctx->ldy * 4, (cuuint64_t)ctx->plane * 4};
+    cuuint32_t box[3] = {(cuuint32_t)kBoxY, (cuuint32_t)(ctx->tile_x + 2 * kRadius), 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = ctx->encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ctx, QP3D_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return QP3D_OK;
+}
+
+static void plan_launch(qp3d_ctx *ctx)
+{
+    const qp3d_geom &g = ctx->g;
+    int ncx = g.nx - 2 * kRadius;
+    int ntx = (ncx + kMaxTileX - 1) / kMaxTileX;
+    ctx->tile_x = (ncx + ntx - 1) / ntx;
+    ctx->nxt = (ncx + ctx->tile_x - 1) / ctx->tile_x;
+    ctx->nyt = (g.ny - kRadius - 1) / kTileY + 1;   // last tile starts below ny-5
+    int ncz = g.nz - 2 * kRadius;
+    long long tiles = (long long)ctx->nxt * ctx->nyt;
+    long long target = 6ll * ctx->nsm;               // ~3 waves at 2 CTAs/SM
+    int nch = (int)((target + tiles - 1) / tiles);
+    int maxch = std::max(1, ncz / 24);
+    nch = std::max(1, std::min(nch, maxch));
+    ctx->chunk_z = (ncz + nch - 1) / nch;
+    ctx->nchunks = (ncz + ctx->chunk_z - 1) / ctx->chunk_z;
+    ctx->smem = plane_smem_bytes(ctx->tile_x, g.pml);
+}
+
+static int alloc_vol(qp3d_ctx *ctx, float **p)
+{
+    CK(cudaMalloc(p, (size_t)ctx->vol * sizeof(float)));
+    return QP3D_OK;
+}
+
+// Copy a dense [nz][nx][ny] host volume into the pitched device layout.
+static int upload_vol(qp3d_ctx *ctx, float *dst, const float *src)
+{
+    const qp3d_geom &g = ctx->g;
+    CK(cudaMemcpy2DAsync(dst, (size_t)ctx->ldy * 4, src, (size_t)g.ny * 4, (size_t)g.ny * 4,
+                         (size_t)g.nx * g.nz, cudaMemcpyHostToDevice, ctx->stream));
+    return QP3D_OK;
+}
+
+static int download_vol(qp3d_ctx *ctx, float *dst, const float *src)
+{
+    const qp3d_geom &g = ctx->g;
+    CK(cudaMemcpy2DAsync(dst, (size_t)g.ny * 4, src, (size_t)ctx->ldy * 4, (size_t)g.ny * 4,
+                         (size_t)g.nx * g.nz, cudaMemcpyDeviceToHost, ctx->stream));
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m)
+{
+    if (!ctx) return QP3D_ERR_ARG;
+    int rc = check_geom(ctx, g);
+    if (rc) return rc;
+    if (!m || !m->vp || !m->epsilon || !m->delta || !m->wavelet || !m->c || !m->c2)
+        return fail(ctx, QP3D_ERR_ARG, "missing model input");
+    if (g->pml > 0 && (!m->dlr || !m->ddlr || !m->dtb || !m->ddtb || !m->dfb || !m->ddfb))
+        return fail(ctx, QP3D_ERR_ARG, "missing PML profiles");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+
+    bool same = ctx->loaded && ctx->g.nx == g->nx && ctx->g.ny == g->ny && ctx->g.nz == g->nz &&
+                ctx->g.nt == g->nt && ctx->g.pml == g->pml;
+    if (!same) free_shot(ctx);
+    ctx->g = *g;
+    ctx->ldy = (g->ny + 31) & ~31;
+    ctx->plane = (long long)g->nx * ctx->ldy;
+    ctx->vol = ctx->plane * g->nz;
+    ctx->hx = g->nx - 2 * g->pml;
+    ctx->hy = g->ny - 2 * g->pml;
+    plan_launch(ctx);
+
+    if (!same) {
+        float **vols[] = {&ctx->U[0], &ctx->U[1], &ctx->K,     &ctx->E2,    &ctx->R8,
+                          &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0], &ctx->W3[1],
+                          &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],  &ctx->W21};
+        for (float **v : vols)
+            if ((rc = alloc_vol(ctx, v))) {
+                free_shot(ctx);
+                return rc;
+            }
+        size_t nrec = (size_t)std::max(g->nt, 1) * ctx->hx * ctx->hy;
+        CK(cudaMalloc(&ctx->record, nrec * sizeof(float)));
+        CK(cudaMalloc(&ctx->gmax, (size_t)std::max(g->nt, 1) * sizeof(float)));
+        CK(cudaMalloc(&ctx->layers, sizeof(float4) * 3 * std::max(g->pml, 1)));
+        if (!ctx->errword) CK(cudaMalloc(&ctx->errword, sizeof(unsigned)));
+    }
+    // model -> per-cell parameters (K, E2, R8 hold vp, eps, delta first)
+    if ((rc = upload_vol(ctx, ctx->K, m->vp)) || (rc = upload_vol(ctx, ctx->E2, m->epsilon)) ||
+        (rc = upload_vol(ctx, ctx->R8, m->delta)))
+        return rc;
+    CK(launch_params(nullptr, nullptr, nullptr, ctx->K, ctx->E2, ctx->R8, ctx->vol, g->dt,
+                     ctx->stream));
+    // coefficient tables
+    derive_coefs(m->c, m->c2, g->dx, g->dy, g->dz, &ctx->coefs);
+    if (g->pml > 0) {
+        std::vector<float4> tab(3 * g->pml);
+        derive_layers(m->dlr, m->ddlr, g->pml, g->dt, tab.data());
+        derive_layers(m->dfb, m->ddfb, g->pml, g->dt, tab.data() + g->pml);
+        derive_layers(m->dtb, m->ddtb, g->pml, g->dt, tab.data() + 2 * g->pml);
+        CK(cudaMemcpyAsync(ctx->layers, tab.data(), sizeof(float4) * tab.size(),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->wavelet.assign(m->wavelet, m->wavelet + g->nt);
+    // sparse source: every non-zero sample (CPU_function.c:326-338 adds all)
+    std::vector<SrcEntry> fused, band, all;
+    if (m->source) {
+        const float *s = m->source;
+        for (int z = 0; z < g->nz; ++z)
+            for (int x = 0; x < g->nx; ++x) {
+                const float *row = s + ((size_t)z * g->nx + x) * g->ny;
+                for (int y = 0; y < g->ny; ++y)
+                    if (row[y] != 0.0f) {
+                        SrcEntry e{x, y, z, row[y]};
+                        all.push_back(e);
+                        bool inside = x >= kRadius && x < g->nx - kRadius && y >= kRadius &&
+                                      y < g->ny - kRadius && z >= kRadius && z < g->nz - kRadius;
+                        (inside ? fused : band).push_back(e);
+                    }
+            }
+    }
+    if (ctx->src_fused) cudaFree(ctx->src_fused);
+    if (ctx->src_band) cudaFree(ctx->src_band);
+    if (ctx->src_all) cudaFree(ctx->src_all);
+    ctx->src_fused = ctx->src_band = ctx->src_all = nullptr;
+    ctx->fuse_sources = fused.size() <= (size_t)kMaxFusedSources;
+    ctx->n_fused = (int)fused.size();
+    ctx->n_band = (int)band.size();
+    ctx->n_all = (int)all.size();
+    auto up = [&](std::vector<SrcEntry> &v, SrcEntry **d) -> int {
+        if (v.empty()) return QP3D_OK;
+        CK(cudaMalloc(d, v.size() * sizeof(SrcEntry)));
+        CK(cudaMemcpy(*d, v.data(), v.size() * sizeof(SrcEntry), cudaMemcpyHostToDevice));
+        return QP3D_OK;
+    };
+    if ((rc = up(fused, &ctx->src_fused)) || (rc = up(band, &ctx->src_band)) ||
+        (rc = up(all, &ctx->src_all)))
+        return rc;
+    // the receiver plane is written by the step kernel when every record cell
+    // lies inside the updated box
+    ctx->rec_fused = g->pml >= kRadius && g->sz >= kRadius && g->sz < g->nz - kRadius &&
+                     ctx->fuse_sources && ctx->n_band == 0;
+    if ((rc = make_tmap(ctx, ctx->U[0], &ctx->tm[0])) || (rc = make_tmap(ctx, ctx->U[1], &ctx->tm[1])))
+        return rc;
+    ctx->loaded = true;
+    return qp3d_shot_reset(ctx);
+}
+
+extern "C" int qp3d_shot_reset(qp3d_ctx *ctx)
+{
+    if (!ctx) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    CK(cudaSetDevice(ctx->device));
+    size_t vb = (size_t)ctx->vol * sizeof(float);
+    float *zero[] = {ctx->U[0], ctx->U[1], ctx->W1[0], ctx->W1[1], ctx->W1[2], ctx->W3[0],
+                     ctx->W3[1], ctx->W3[2], ctx->P[0],  ctx->P[1],  ctx->P[2],  ctx->W21};
+    for (float *p : zero) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
+    CK(cudaMemsetAsync(ctx->gmax, 0, sizeof(float) * std::max(ctx->g.nt, 1), ctx->stream));
+    CK(cudaMemsetAsync(ctx->record, 0,
+                       sizeof(float) * (size_t)std::max(ctx->g.nt, 1) * ctx->hx * ctx->hy,
+                       ctx->stream));
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(unsigned), ctx->stream));
+    ctx->step = 0;
+    ctx->cur = 0;
+    return QP3D_OK;
+}
+
+// Enqueue one time step.  ev_* are optional events bracketing the kernels.
+static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cudaEvent_t ev_s0,
+                        cudaEvent_t ev_s1)
+{
+    const qp3d_geom &g = ctx->g;
+    const int k = ctx->step;
+    const int a = ctx->cur, b = a ^ 1;
+    PlaneParams p;
+    memset(&p, 0, sizeof(p));
+    p.nx = g.nx; p.ny = g.ny; p.nz = g.nz; p.ldy = ctx->ldy; p.pml = g.pml; p.sz = g.sz;
+    p.tile_x = ctx->tile_x;
+    p.chunk_z = ctx->chunk_z;
+    p.plane = ctx->plane;
+    p.k = ctx->coefs;
+    p.dt = g.dt;
+    p.step = k;
+    p.wavelet = ctx->wavelet[k];
+    p.u_io = ctx->U[b];
+    p.prm_k = ctx->K; p.prm_e = ctx->E2; p.prm_r = ctx->R8;
+    const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
+    p.w1o = ctx->W1[lo]; p.w1c = ctx->W1[lc]; p.w1n = ctx->W1[ln];
+    p.w3o = ctx->W3[lo]; p.w3c = ctx->W3[lc]; p.w3n = ctx->W3[ln];
+    p.po = ctx->P[lo];   p.pc = ctx->P[lc];   p.pn = ctx->P[ln];
+    p.w21 = ctx->W21;
+    p.layers = ctx->layers;
+    p.gmax = ctx->gmax + k;
+    p.gmax_bits = reinterpret_cast<unsigned *>(ctx->gmax + k);
+    float *rec_plane = ctx->record + (size_t)k * ctx->hx * ctx->hy;
+    p.record = ctx->rec_fused ? rec_plane : nullptr;
+    p.src = ctx->fuse_sources ? ctx->src_fused : nullptr;
+    p.nsrc = ctx->fuse_sources ? ctx->n_fused : 0;
+    p.err = ctx->errword;
+    dim3 grid(ctx->nyt, ctx->nxt, ctx->nchunks);
+
+    if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
+    CK(launch_gradmax(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
+    if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
+    if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
+    CK(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
+    if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
+    if (ctx->fuse_sources) {
+        CK(launch_band_sources(ctx->U[b], ctx->U[a], ctx->src_band, ctx->n_band, ctx->plane,
+                               ctx->ldy, p.wavelet, ctx->stream));
+    } else {
+        CK(launch_all_sources(ctx->U[b], ctx->U[a], ctx->src_all, ctx->n_all, ctx->plane, ctx->ldy,
+                              g.nx, g.ny, g.nz, p.wavelet, ctx->stream));
+    }
+    if (!ctx->rec_fused)
+        CK(launch_record(ctx->U[b], rec_plane, g.nx, g.ny, g.pml, g.sz, ctx->ldy, ctx->plane,
+                         ctx->stream));
+    ctx->cur = b;
+    ctx->step = k + 1;
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_launches_per_step(const qp3d_ctx *ctx)
+{
+    if (!ctx || !ctx->loaded) return 0;
+    int n = 2;
+    if (ctx->fuse_sources) n += ctx->n_band > 0 ? 1 : 0;
+    else n += ctx->n_all > 0 ? 1 : 0;
+    if (!ctx->rec_fused) n += 1;
+    return n;
+}
+
+extern "C" int qp3d_shot_advance(qp3d_ctx *ctx, int nsteps)
+{
+    if (!ctx || nsteps < 0) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (ctx->step + nsteps > ctx->g.nt)
+        return fail(ctx, QP3D_ERR_ARG, "advance past nt (%d + %d > %d)", ctx->step, nsteps, ctx->g.nt);
+    CK(cudaSetDevice(ctx->device));
+    for (int i = 0; i < nsteps; ++i) {
+        int rc = enqueue_step(ctx, nullptr, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+    }
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_sync(qp3d_ctx *ctx)
+{
+    if (!ctx) return QP3D_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->errword) {
+        unsigned e = 0;
+        CK(cudaMemcpy(&e, ctx->errword, sizeof(e), cudaMemcpyDeviceToHost));
+        if (e) return fail(ctx, QP3D_ERR_TIMEOUT, "device wait timed out (flags 0x%x)", e);
+    }
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_step(const qp3d_ctx *ctx) { return ctx ? ctx->step : -1; }
+
+extern "C" int qp3d_shot_read_record(qp3d_ctx *ctx, int k0, int nsteps, float *out)
+{
+    if (!ctx || !out || k0 < 0 || nsteps < 0) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (k0 + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "record range past nt");
+    int rc = qp3d_shot_sync(ctx);
+    if (rc) return rc;
+    size_t row = (size_t)ctx->hx * ctx->hy;
+    CK(cudaMemcpy(out, ctx->record + (size_t)k0 * row, row * nsteps * sizeof(float),
+                  cudaMemcpyDeviceToHost));
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_read_uxyzmax(qp3d_ctx *ctx, int k0, int nsteps, float *out)
+{
+    if (!ctx || !out || k0 < 0 || nsteps < 0) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (k0 + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "range past nt");
+    int rc = qp3d_shot_sync(ctx);
+    if (rc) return rc;
+    CK(cudaMemcpy(out, ctx->gmax + k0, nsteps * sizeof(float), cudaMemcpyDeviceToHost));
+    return QP3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// State in the reference layout
+// ---------------------------------------------------------------------------
+namespace {
+struct FaceLayout {
+    size_t fsz[6];
+    size_t off[6][10];
+    size_t total;
+};
+FaceLayout face_layout(int nx, int ny, int nz, int pml)
+{
+    FaceLayout L;
+    size_t xf = (size_t)pml * ny * nz, yf = (size_t)pml * nx * nz, zf = (size_t)pml * nx * ny;
+    size_t s[6] = {xf, xf, yf, yf, zf, zf};
+    size_t o = 0;
+    for (int f = 0; f < 6; f++) {
+        L.fsz[f] = s[f];
+        for (int a = 0; a < 10; a++) {
+            L.off[f][a] = o;
+            o += s[f];
+        }
+    }
+    L.total = o;
+    return L;
+}
+// cell (z,x,y) -> face-local index, or -1 when the cell is not in face f
+long long face_index(int f, int z, int x, int y, int nx, int ny, int nz, int pml)
+{
+    switch (f) {
+    case 0: return x < pml ? (long long)z * ny * pml + (long long)x * ny + y : -1;
+    case 1: return x >= nx - pml ? (long long)z * ny * pml + (long long)(x - nx + pml) * ny + y : -1;
+    case 2: return y < pml ? (long long)z * nx * pml + (long long)x * pml + y : -1;
+    case 3: return y >= ny - pml ? (long long)z * nx * pml + (long long)x * pml + (y - ny + pml) : -1;
+    case 4: return z < pml ? (long long)z * nx * ny + (long long)x * ny + y : -1;
+    default: return z >= nz - pml ? (long long)(z - nz + pml) * ny * nx + (long long)x * ny + y : -1;
+    }
+}
+int region(int x, int y, int z, int nx, int ny, int nz, int pml)
+{
+    if (x < pml) return 0;
+    if (x >= nx - pml) return 1;
+    if (y < pml) return 2;
+    if (y >= ny - pml) return 3;
+    if (z < pml) return 4;
+    if (z >= nz - pml) return 5;
+    return -1;
+}
+}  // namespace
+
+extern "C" size_t qp3d_pml_state_size(int nx, int ny, int nz, int pml)
+{
+    if (nx <= 0 || ny <= 0 || nz <= 0 || pml < 0) return 0;
+    return face_layout(nx, ny, nz, pml).total;
+}
+
+// shadow-volume arrays in the order of the face arrays (w11..p3) for step k
+static void level_arrays(qp3d_ctx *ctx, int k, float *arr[10])
+{
+    const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
+    arr[0] = ctx->W1[lo]; arr[1] = ctx->W1[lc]; arr[2] = ctx->W1[ln]; arr[3] = ctx->W21;
+    arr[4] = ctx->W3[lo]; arr[5] = ctx->W3[lc]; arr[6] = ctx->W3[ln];
+    arr[7] = ctx->P[lo];  arr[8] = ctx->P[lc];  arr[9] = ctx->P[ln];
+}
+
+extern "C" int qp3d_shot_write_state(qp3d_ctx *ctx, int step, const float *u_prev,
+                                     const float *u_cur, const float *pml_state)
+{
+    if (!ctx) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (step < 0 || step > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "step out of range");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->step = step;
+    int rc;
+    if (u_prev && (rc = upload_vol(ctx, ctx->U[ctx->cur ^ 1], u_prev))) return rc;
+    if (u_cur && (rc = upload_vol(ctx, ctx->U[ctx->cur], u_cur))) return rc;
+    if (pml_state) {
+        const qp3d_geom &g = ctx->g;
+        FaceLayout L = face_layout(g.nx, g.ny, g.nz, g.pml);
+        float *arr[10];
+        level_arrays(ctx, step, arr);
+        std::vector<float> tmp((size_t)ctx->vol);
+        for (int a = 0; a < 10; ++a) {
+            std::fill(tmp.begin(), tmp.end(), 0.0f);
+            for (int z = 0; z < g.nz; ++z)
+                for (int x = 0; x < g.nx; ++x)
+                    for (int y = 0; y < g.ny; ++y) {
+                        int f = region(x, y, z, g.nx, g.ny, g.nz, g.pml);
+                        if (f < 0) continue;
+                        long long fi = face_index(f, z, x, y, g.nx, g.ny, g.nz, g.pml);
+                        tmp[(size_t)z * ctx->plane + (size_t)x * ctx->ldy + y] =
+                            pml_state[L.off[f][a] + fi];
+                    }
+            CK(cudaMemcpy(arr[a], tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_read_state(qp3d_ctx *ctx, float *u_prev, float *u_cur, float *pml_state)
+{
+    if (!ctx) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    int rc = qp3d_shot_sync(ctx);
+    if (rc) return rc;
+    if (u_prev && (rc = download_vol(ctx, u_prev, ctx->U[ctx->cur ^ 1]))) return rc;
+    if (u_cur && (rc = download_vol(ctx, u_cur, ctx->U[ctx->cur]))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (pml_state) {
+        const qp3d_geom &g = ctx->g;
+        FaceLayout L = face_layout(g.nx, g.ny, g.nz, g.pml);
+        memset(pml_state, 0, L.total * sizeof(float));
+        // levels as the next step will read them: w11 = w(k-1), w12 = w(k)
+        float *arr[10];
+        level_arrays(ctx, ctx->step, arr);
+        std::vector<float> tmp((size_t)ctx->vol);
+        for (int a = 0; a < 10; ++a) {
+            CK(cudaMemcpy(tmp.data(), arr[a], tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            for (int z = 0; z < g.nz; ++z)
+                for (int x = 0; x < g.nx; ++x)
+                    for (int y = 0; y < g.ny; ++y) {
+                        int f = region(x, y, z, g.nx, g.ny, g.nz, g.pml);
+                        if (f < 0) continue;
+                        long long fi = face_index(f, z, x, y, g.nx, g.ny, g.nz, g.pml);
+                        pml_state[L.off[f][a] + fi] =
+                            tmp[(size_t)z * ctx->plane + (size_t)x * ctx->ldy + y];
+                    }
+        }
+        // after the reference's exchange w13 == w12, w33 == w32, p3 == p2
+        for (int f = 0; f < 6; ++f) {
+            memcpy(pml_state + L.off[f][2], pml_state + L.off[f][1], L.fsz[f] * sizeof(float));
+            memcpy(pml_state + L.off[f][6], pml_state + L.off[f][5], L.fsz[f] * sizeof(float));
+            memcpy(pml_state + L.off[f][9], pml_state + L.off[f][8], L.fsz[f] * sizeof(float));
+        }
+    }
+    return QP3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Snapshots
+// ---------------------------------------------------------------------------
+static int ensure_snap(qp3d_ctx *ctx, size_t n)
+{
+    if (n <= ctx->snap_cap) return QP3D_OK;
+    if (ctx->snap_dev) cudaFree(ctx->snap_dev);
+    if (ctx->snap_host) cudaFreeHost(ctx->snap_host);
+    ctx->snap_dev = nullptr;
+    ctx->snap_host = nullptr;
+    ctx->snap_cap = 0;
+    CK(cudaMalloc(&ctx->snap_dev, n * sizeof(float)));
+    CK(cudaMallocHost(&ctx->snap_host, n * sizeof(float)));
+    ctx->snap_cap = n;
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap)
+{
+    if (!ctx || !snap || !snap->fn) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    const qp3d_geom &g = ctx->g;
+    const int pml = g.pml, hx = ctx->hx, hy = ctx->hy, hz = g.nz - 2 * pml;
+    const float *u = ctx->U[ctx->cur];
+    const int k = ctx->step - 1;
+    struct Req { int kind, x0, x1, y0, y1, z0, z1, n0, n1, n2; };
+    Req reqs[4] = {
+        {QP3D_SNAP_VOLUME, pml, pml + hx, pml, pml + hy, pml, pml + hz, hz, hx, hy},
+        {QP3D_SNAP_XZ, pml, pml + hx, pml + (hy - 1) / 2, pml + (hy - 1) / 2 + 1, pml, pml + hz, hz, hx, 1},
+        {QP3D_SNAP_YZ, pml + (hx - 1) / 2, pml + (hx - 1) / 2 + 1, pml, pml + hy, pml, pml + hz, hz, hy, 1},
+        {QP3D_SNAP_XY, pml, pml + hx, pml, pml + hy, pml + (hz - 1) / 2, pml + (hz - 1) / 2 + 1, hx, hy, 1},
+    };
+    for (const Req &r : reqs) {
+        if (!(snap->kinds & (1u << r.kind))) continue;
+        size_t n = (size_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
+        int rc = ensure_snap(ctx, n);
+        if (rc) return rc;
+        CK(launch_crop(u, ctx->snap_dev, r.x0, r.x1, r.y0, r.y1, r.z0, r.z1, ctx->ldy, ctx->plane,
+                       ctx->stream));
+        CK(cudaMemcpyAsync(ctx->snap_host, ctx->snap_dev, n * sizeof(float), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        rc = qp3d_shot_sync(ctx);
+        if (rc) return rc;
+        if (snap->fn(snap->user, k, r.kind, ctx->snap_host, r.n0, r.n1, r.n2) != 0)
+            return fail(ctx, QP3D_ERR_CALLBACK, "snapshot callback failed at step %d", k);
+    }
+    return QP3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int qp3d_forward(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m, float *record,
+                            const qp3d_snap *snap)
+{
+    if (!ctx || !record) return QP3D_ERR_ARG;
+    int rc = qp3d_shot_load(ctx, g, m);
+    if (rc) return rc;
+    const bool snaps = snap && snap->fn && snap->ntsnap > 0 && snap->kinds;
+    int k = 0;
+    while (k < g->nt) {
+        int n = g->nt - k;
+        if (snaps) {
+            // the reference snapshots after step k when k % ntsnap == 0
+            int next = (k % snap->ntsnap == 0) ? k : (k / snap->ntsnap + 1) * snap->ntsnap;
+            n = std::min(n, next - k + 1);
+        }
+        if ((rc = qp3d_shot_advance(ctx, n))) return rc;
+        k += n;
+        if (snaps && (k - 1) % snap->ntsnap == 0)
+            if ((rc = qp3d_shot_snapshot(ctx, snap))) return rc;
+    }
+    return qp3d_shot_read_record(ctx, 0, g->nt, record);
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int qp3d_shot_time(qp3d_ctx *ctx, int nsteps, float *ms_total, float *ms_step,
+                              float *ms_gradmax)
+{
+    if (!ctx || nsteps < 0) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (ctx->step + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "advance past nt");
+    CK(cudaSetDevice(ctx->device));
+    const bool per_kernel = ms_step || ms_gradmax;
+    std::vector<cudaEvent_t> evs;
+    if (per_kernel) {
+        evs.resize((size_t)4 * nsteps);
+        for (auto &e : evs) CK(cudaEventCreate(&e));
+    }
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    for (int i = 0; i < nsteps; ++i) {
+        int rc = per_kernel ? enqueue_step(ctx, evs[4 * i], evs[4 * i + 1], evs[4 * i + 2], evs[4 * i + 3])
+                            : enqueue_step(ctx, nullptr, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    int rc = qp3d_shot_sync(ctx);
+    if (rc) return rc;
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+    if (ms_total) *ms_total = t;
+    if (per_kernel) {
+        float sg = 0, ss = 0;
+        for (int i = 0; i < nsteps; ++i) {
+            float a = 0, b = 0;
+            CK(cudaEventElapsedTime(&a, evs[4 * i], evs[4 * i + 1]));
+            CK(cudaEventElapsedTime(&b, evs[4 * i + 2], evs[4 * i + 3]));
+            sg += a;
+            ss += b;
+        }
+        for (auto &e : evs) cudaEventDestroy(e);
+        if (ms_step) *ms_step = ss;
+        if (ms_gradmax) *ms_gradmax = sg;
+    }
+    return QP3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int qp3d_event_record(qp3d_ctx *ctx, int slot)
+{
+    if (!ctx || slot < 0 || slot >= 8) return QP3D_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventRecord(ctx->uev[slot], ctx->stream));
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_event_elapsed(qp3d_ctx *ctx, int a, int b, float *ms)
+{
+    if (!ctx || !ms || a < 0 || a >= 8 || b < 0 || b >= 8) return QP3D_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventSynchronize(ctx->uev[b]));
+    CK(cudaEventElapsedTime(ms, ctx->uev[a], ctx->uev[b]));
+    return QP3D_OK;
+}
+
+extern "C" void *qp3d_host_alloc(size_t bytes)
+{
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+    return p;
+}
+
+extern "C" void qp3d_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}

@@ -1,0 +1,103 @@
+// qp3d_internal.h -- shared definitions between the host API and the kernels.
+//
+// Device layout of one shot (all float32, row pitch ldy = ny rounded up to 32
+// so every row starts on a 128-byte boundary):
+//   U[2]            wavefields; U[cur] is u(k) ("u2"), U[cur^1] holds u(k-1)
+//                   on entry to a step and u(k+1) on exit (updated in place)
+//   K, E2, R8       per-cell parameters (vp*dt)^2, 2*eps, 8*(eps-delta)
+//   W1[3],W3[3],P[3] PML split fields, three time levels each, rotated by
+//                   index (no copies); W21 is updated in place.  These are
+//                   full "shadow" volumes: only PML cells are ever touched,
+//                   so a cell's state lives at the cell's own index whatever
+//                   face owns it.
+//   record          nt * hx * hy receiver samples
+//   gmax            nt floats: max|grad u| of each step (bits, atomicMax)
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qp3d {
+
+constexpr int kRadius = 5;        // 10th-order stencil (M/2 with M = 10)
+constexpr int kTileY = 32;        // y cells per tile = 8 quads of 4 cells
+constexpr int kQuadsY = kTileY / 4;
+constexpr int kHaloY = 8;         // y halo rounded up to 16 bytes
+constexpr int kBoxY = kTileY + 2 * kHaloY;   // 48 floats per staged row
+constexpr int kPrefetch = 2;      // planes loaded ahead of use
+constexpr int kRing = 2 * kRadius + 1 + kPrefetch;   // staged planes
+constexpr int kMaxTileX = 32;
+constexpr int kThreads = kQuadsY * kMaxTileX;        // 256
+constexpr int kMaxFusedSources = 64;
+constexpr int kMaxPml = 256;
+
+// Error bits written to the device error word.
+constexpr unsigned kErrWaitTimeout = 1u;
+
+struct Coefs {
+    float cx[kRadius], cy[kRadius], cz[kRadius];      // c[31+m]/h
+    float c2x[kRadius], c2y[kRadius], c2z[kRadius];   // c2[31+m]/h^2
+    float kx, ky, kz;                                  // -2*sum(c2?)
+};
+
+// One source sample: padded coordinates and the amplitude.
+struct SrcEntry {
+    int x, y, z;
+    float v;
+};
+
+struct PlaneParams {
+    // geometry
+    int nx, ny, nz, ldy, pml, sz;
+    int tile_x;          // rows per tile (<= kMaxTileX)
+    int chunk_z;         // planes per z chunk
+    long long plane;     // nx * ldy
+    Coefs k;
+    float dt;
+    int step;            // time step index k
+    float wavelet;       // wavelet[k]
+    // buffers
+    float *u_io;         // u(k-1) in, u(k+1) out (in place)
+    const float *prm_k, *prm_e, *prm_r;
+    const float *w1o, *w1c; float *w1n;   // w11, w12 -> w13
+    const float *w3o, *w3c; float *w3n;   // w31, w32 -> w33
+    const float *po, *pc; float *pn;      // p1, p2 -> p3
+    float *w21;
+    const float4 *layers;     // [3][pml] (a1, a2, a3, dd) for lr, fb, tb
+    const float *gmax;        // &gmax[step]
+    unsigned *gmax_bits;      // &gmax[step] as bits (gradmax kernel)
+    float *record;            // record plane of this step, or null
+    const SrcEntry *src;      // sources inside the updated box, fused
+    int nsrc;
+    unsigned *err;
+};
+
+struct Shot;   // host-side, defined in qp3d_api.cu
+
+// Launchers (qp3d_kernels.cu).  All enqueue on `stream` and return the
+// launch error.
+cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p,
+                           dim3 grid, size_t smem, cudaStream_t stream);
+cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p,
+                        dim3 grid, size_t smem, cudaStream_t stream);
+cudaError_t launch_band_sources(float *u_new, const float *u_cur,
+                                const SrcEntry *src, int n, long long plane,
+                                int ldy, float w, cudaStream_t stream);
+cudaError_t launch_all_sources(float *u_new, const float *u_cur,
+                               const SrcEntry *src, int n, long long plane,
+                               int ldy, int nx, int ny, int nz, float w,
+                               cudaStream_t stream);
+cudaError_t launch_record(const float *u, float *rec, int nx, int ny, int pml,
+                          int sz, int ldy, long long plane,
+                          cudaStream_t stream);
+cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0,
+                        int y1, int z0, int z1, int ldy, long long plane,
+                        cudaStream_t stream);
+cudaError_t launch_params(const float *vp, const float *eps, const float *del,
+                          float *K, float *E2, float *R8, long long n, float dt,
+                          cudaStream_t stream);
+size_t plane_smem_bytes(int tile_x, int pml);
+cudaError_t configure_kernels();
+
+}  // namespace qp3d

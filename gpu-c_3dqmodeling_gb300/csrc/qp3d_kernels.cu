@@ -1,0 +1,747 @@
+// qp3d_kernels.cu -- sm_103a kernels for the 3D pure-qP VTI time step.
+//
+// One time step of the reference (3dPureqPModeling_single_shot.cu:282-320:
+// grad -> D2H + host absMaxval -> scalar_operator -> wavefield_update ->
+// addsource -> exchange -> D2H + record crop) becomes two kernels:
+//
+//   qp3d_gradmax_kernel   max over [5,n-5)^3 of |du/dx|,|du/dy|,|du/dz| of
+//                         u(k) (GPU_kernel.cu:14-33 + CPU_function.c:10-22),
+//                         reduced on the device with atomicMax on the float
+//                         bits (all values are >= 0, so the bit order is the
+//                         value order).
+//   qp3d_step_kernel      everything else in one pass: gradient, scalar
+//                         operator S (GPU_kernel.cu:87-115), Laplacians,
+//                         interior leapfrog and the six split-field PML faces
+//                         (GPU_kernel.cu:534-639), source injection
+//                         (GPU_kernel.cu:720-731) and the receiver plane
+//                         (3dPureqPModeling_single_shot.cu:333-337).  The
+//                         time-level rotation (GPU_kernel.cu:733-812) is done
+//                         by the host swapping buffer indices.
+//
+// Both kernels march along z.  A CTA owns a tile of tile_x rows (x) by 32
+// cells (y) and a chunk of z planes.  Each thread owns one row and four
+// consecutive y cells (a "quad", one float4).  Planes of u(k), with a 5-row
+// and 8-column halo, are staged into a ring of kRing shared-memory slots by
+// TMA (cp.async.bulk.tensor.3d) and completed on one mbarrier per slot; the
+// stencil reads all 30 taps from shared memory.  Loads of the next planes
+// overlap the arithmetic of the current one.
+//
+// Arithmetic.  The 1/h factors of the reference (each tap divided by dx or
+// dx*dx, CPU_function.c:314-316,393-395) are folded into the coefficient
+// tables, and a*b+c is fused where written as fmaf().  This translation unit
+// is compiled with -fmad=false so that no other fusion happens: the result is
+// bit-identical to the mirror variant of the CPU oracle.  Division and square
+// root are IEEE (div.rn / sqrt.rn).
+#include "qp3d_internal.h"
+
+#include <math.h>
+
+namespace qp3d {
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + TMA
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up after ~2 s of wall time.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    unsigned long long t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > 2000000000ull) return false;
+    }
+}
+
+__device__ __forceinline__ void fence_barrier_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, int c0, int c1,
+                                            int c2, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float4 lds4(const float *p)
+{
+    return *reinterpret_cast<const float4 *>(p);
+}
+
+__device__ __forceinline__ float f4(const float4 &v, int j)
+{
+    return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w;
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory layout of both plane kernels
+// ---------------------------------------------------------------------------
+struct SmemLayout {
+    size_t slot_floats;   // one staged plane, padded to 128 B
+    size_t ring_bytes;
+    size_t bar_off;       // kRing mbarriers
+    size_t tab_off;       // 3 * pml float4 layer coefficients
+    size_t src_off;       // fused source entries of this CTA
+    size_t misc_off;      // scalars
+    size_t total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int tile_x, int pml)
+{
+    SmemLayout L;
+    size_t box = (size_t)(tile_x + 2 * kRadius) * kBoxY;
+    L.slot_floats = (box + 31) & ~(size_t)31;
+    L.ring_bytes = L.slot_floats * 4 * kRing;
+    L.bar_off = L.ring_bytes;
+    L.tab_off = L.bar_off + 8 * kRing;
+    L.tab_off = (L.tab_off + 15) & ~(size_t)15;
+    L.src_off = L.tab_off + 16 * 3 * (size_t)(pml > 0 ? pml : 1);
+    L.misc_off = L.src_off + sizeof(SrcEntry) * kMaxFusedSources;
+    L.misc_off = (L.misc_off + 15) & ~(size_t)15;
+    L.total = L.misc_off + 64;
+    return L;
+}
+
+size_t plane_smem_bytes(int tile_x, int pml) { return smem_layout(tile_x, pml).total; }
+
+// ---------------------------------------------------------------------------
+// Threshold of the scalar operator, GPU_kernel.cu:99.
+//   (double)mode > 1.0e-02 * uxyzMax  <=>  mode > Tf, Tf = largest float not
+//   above the double product;  mode = sqrtf(m2) > Tf  <=>  m2 > T2 with
+//   T2 = max{x : sqrtf(x) <= Tf}.  The oracle derives T2 the same way.
+// ---------------------------------------------------------------------------
+__device__ float threshold_m2(float gmax)
+{
+    double td = 1.0e-02 * (double)gmax;
+    float t = __double2float_rd(td);
+    if (!(t >= 0.0f)) return t;
+    float x = __fmul_rn(t, t);
+    for (int it = 0; it < 64 && x > 0.0f && __fsqrt_rn(x) > t; ++it) x = nextafterf(x, 0.0f);
+    for (int it = 0; it < 64; ++it) {
+        float n = nextafterf(x, INFINITY);
+        if (isinf(n) || __fsqrt_rn(n) > t) break;
+        x = n;
+    }
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// Region of a cell: -1 interior, else the PML face by the reference priority
+// left, right, forward, backward, top, bottom (GPU_kernel.cu:558-626).
+// ---------------------------------------------------------------------------
+enum { F_L = 0, F_R, F_F, F_BK, F_T, F_BO };
+
+__device__ __forceinline__ int region_of(int x, int y, int z, int nx, int ny, int nz, int pml)
+{
+    if (x < pml) return F_L;
+    if (x >= nx - pml) return F_R;
+    if (y < pml) return F_F;
+    if (y >= ny - pml) return F_BK;
+    if (z < pml) return F_T;
+    if (z >= nz - pml) return F_BO;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Stencil over one quad: first and second derivatives along x, y, z of the
+// four cells (x, y..y+3, z) from the staged planes.
+// ---------------------------------------------------------------------------
+template <bool SECOND>
+__device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_floats, int t, int rc,
+                                            const Coefs &k, float Ux[4], float Uy[4],
+                                            float Uz[4], float Uxx[4], float Uyy[4],
+                                            float Uzz[4], float u0[4])
+{
+    const float *pc = ring + (size_t)((t + kRadius) % kRing) * slot_floats;
+    // y taps: columns c-8 .. c+11 of the centre plane
+    float Y[20];
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+        float4 v = lds4(pc + rc - 8 + 4 * b);
+        Y[4 * b] = v.x; Y[4 * b + 1] = v.y; Y[4 * b + 2] = v.z; Y[4 * b + 3] = v.w;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float c0 = Y[8 + j];
+        u0[j] = c0;
+        float g = 0.0f, l = 0.0f;
+        if (SECOND) l = __fmul_rn(k.ky, c0);
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m) {
+            float a = Y[8 + j + m + 1], b = Y[8 + j - m - 1];
+            float d = __fsub_rn(a, b);
+            g = (m == 0) ? __fmul_rn(k.cy[0], d) : fmaf(k.cy[m], d, g);
+            if (SECOND) l = fmaf(k.c2y[m], __fadd_rn(a, b), l);
+        }
+        Uy[j] = g;
+        if (SECOND) Uyy[j] = l;
+    }
+    // x taps: rows r +- m of the centre plane
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        Ux[j] = 0.0f;
+        if (SECOND) Uxx[j] = __fmul_rn(k.kx, u0[j]);
+    }
+#pragma unroll
+    for (int m = 0; m < kRadius; ++m) {
+        float4 a = lds4(pc + rc + (m + 1) * kBoxY);
+        float4 b = lds4(pc + rc - (m + 1) * kBoxY);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float av = f4(a, j), bv = f4(b, j);
+            float d = __fsub_rn(av, bv);
+            Ux[j] = (m == 0) ? __fmul_rn(k.cx[0], d) : fmaf(k.cx[m], d, Ux[j]);
+            if (SECOND) Uxx[j] = fmaf(k.c2x[m], __fadd_rn(av, bv), Uxx[j]);
+        }
+    }
+    // z taps: planes t+5 +- m
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        Uz[j] = 0.0f;
+        if (SECOND) Uzz[j] = __fmul_rn(k.kz, u0[j]);
+    }
+#pragma unroll
+    for (int m = 0; m < kRadius; ++m) {
+        const float *pp = ring + (size_t)((t + kRadius + m + 1) % kRing) * slot_floats;
+        const float *pm = ring + (size_t)((t + kRadius - m - 1) % kRing) * slot_floats;
+        float4 a = lds4(pp + rc);
+        float4 b = lds4(pm + rc);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float av = f4(a, j), bv = f4(b, j);
+            float d = __fsub_rn(av, bv);
+            Uz[j] = (m == 0) ? __fmul_rn(k.cz[0], d) : fmaf(k.cz[m], d, Uz[j]);
+            if (SECOND) Uzz[j] = fmaf(k.c2z[m], __fadd_rn(av, bv), Uzz[j]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Common pipeline: prologue (barriers, first loads) and the per-plane wait /
+// refill.  Returns false when a wait timed out (error bit set).
+// ---------------------------------------------------------------------------
+struct Pipe {
+    float *ring;
+    uint64_t *bar;
+    size_t slot_floats;
+    unsigned box_bytes;
+    int nplanes;     // planes to stage for this chunk
+    int zfirst;      // z of staged plane 0
+    int c0, c1;      // TMA coordinates of the box (y, x)
+};
+
+__device__ __forceinline__ void pipe_issue(const Pipe &P, const CUtensorMap *tm, int i)
+{
+    int s = i % kRing;
+    mbar_arrive_expect_tx(&P.bar[s], P.box_bytes);
+    tma_load_3d(P.ring + (size_t)s * P.slot_floats, tm, P.c0, P.c1, P.zfirst + i, &P.bar[s]);
+}
+
+__device__ __forceinline__ bool pipe_wait(const Pipe &P, int i)
+{
+    return mbar_wait_bounded(&P.bar[i % kRing], (unsigned)((i / kRing) & 1));
+}
+
+// After an aborted loop: wait (bounded) for every load still in flight so
+// that no TMA write lands in shared memory after the CTA has exited.
+__device__ void pipe_drain(const Pipe &P, int first_unwaited, int issued)
+{
+    for (int i = first_unwaited; i < issued; ++i) (void)pipe_wait(P, i);
+}
+
+// ---------------------------------------------------------------------------
+// gradmax kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 2)
+    qp3d_gradmax_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const SmemLayout L = smem_layout(p.tile_x, p.pml);
+    Pipe P;
+    P.ring = reinterpret_cast<float *>(smem);
+    P.bar = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+    P.slot_floats = L.slot_floats;
+    P.box_bytes = (unsigned)((p.tile_x + 2 * kRadius) * kBoxY * 4);
+
+    const int tid = threadIdx.x;
+    const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
+    const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
+    const int z0 = kRadius + blockIdx.z * p.chunk_z;
+    const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
+    if (z0 >= z1) return;
+    const int nzc = z1 - z0;
+    P.nplanes = nzc + 2 * kRadius;
+    P.zfirst = z0 - kRadius;
+    P.c0 = y0 - kHaloY;
+    P.c1 = x0 - kRadius;
+
+    const int x = x0 + r, yq = y0 + 4 * q;
+    const bool row_ok = (r < p.tile_x) && (x < p.nx - kRadius);
+    bool cell_ok[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < p.ny - kRadius);
+    const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
+
+    if (tid == 0) {
+        for (int s = 0; s < kRing; ++s) mbar_init(&P.bar[s], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    int issued = 0;
+    if (tid == 0) {
+        issued = min(kRing, P.nplanes);
+        for (int i = 0; i < issued; ++i) pipe_issue(P, &tm_u, i);
+    }
+
+    float mx = 0.0f;
+    bool ok = true;
+    int waited = 0;   // planes [0, waited) are complete (thread-local view)
+    for (int t = 0; t < nzc; ++t) {
+        int need = t + 2 * kRadius;
+        while (ok && waited <= need) {
+            ok = pipe_wait(P, waited);
+            if (ok) ++waited;
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(p.err, kErrWaitTimeout);
+            break;
+        }
+        if (row_ok) {
+            float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+            quad_derivs<false>(P.ring, P.slot_floats, t, rc, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (cell_ok[j])
+                    mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+        }
+        __syncthreads();
+        if (tid == 0 && t + kRing < P.nplanes) {
+            fence_proxy_async();
+            pipe_issue(P, &tm_u, t + kRing);
+            issued = t + kRing + 1;
+        }
+    }
+    if (!ok && tid == 0) pipe_drain(P, waited, issued);
+    // warp reduce, one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0 && mx > 0.0f) atomicMax(p.gmax_bits, __float_as_uint(mx));
+}
+
+// ---------------------------------------------------------------------------
+// PML update of one cell (GPU_kernel.cu:566-637 restated with per-layer
+// coefficients a1 = (d*dt+1)^2-3, a2 = 2*d*dt-1, a3 = 1-dt*d).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float pml_cell(int f, float4 lc, float KS, float e2, float Ux,
+                                          float Uy, float Uz, float Uxx, float Uyy, float Uzz,
+                                          float dt, float w11, float w12, float w21, float w31,
+                                          float w32, float p1, float p2, float &nw13,
+                                          float &nw21, float &nw33, float &np3)
+{
+    const bool isx = (f == F_L || f == F_R), isy = (f == F_F || f == F_BK);
+    const float e2KS = __fmul_rn(e2, KS);
+    const float A = (isx || isy) ? e2KS : KS;
+    const float Unn = isx ? Uxx : (isy ? Uyy : Uzz);
+    const float Un = isx ? Ux : (isy ? Uy : Uz);
+    const float Bt = (isx || isy) ? KS : e2KS;
+    const float Tt = isx ? fmaf(e2, Uyy, Uzz) : (isy ? fmaf(e2, Uxx, Uzz) : __fadd_rn(Uxx, Uyy));
+    const float a1 = lc.x, a2 = lc.y, a3 = lc.z, dd = lc.w;
+    nw13 = fmaf(A, Unn, fmaf(-a1, w12, __fmul_rn(a2, w11)));
+    float Ad = __fmul_rn(A, dd);
+    if (f == F_R || f == F_BK || f == F_BO) Ad = -Ad;
+    np3 = fmaf(Ad, Un, fmaf(-a1, p2, __fmul_rn(a2, p1)));
+    nw21 = fmaf(dt, np3, __fmul_rn(a3, w21));
+    nw33 = fmaf(Bt, Tt, fmaf(2.0f, w32, -w31));
+    return __fadd_rn(__fadd_rn(nw13, nw21), nw33);
+}
+
+// ---------------------------------------------------------------------------
+// step kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 2)
+    qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const SmemLayout L = smem_layout(p.tile_x, p.pml);
+    Pipe P;
+    P.ring = reinterpret_cast<float *>(smem);
+    P.bar = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+    P.slot_floats = L.slot_floats;
+    P.box_bytes = (unsigned)((p.tile_x + 2 * kRadius) * kBoxY * 4);
+    float4 *tab = reinterpret_cast<float4 *>(smem + L.tab_off);
+    SrcEntry *csrc = reinterpret_cast<SrcEntry *>(smem + L.src_off);
+    float *misc = reinterpret_cast<float *>(smem + L.misc_off);
+    int *misc_i = reinterpret_cast<int *>(smem + L.misc_off + 16);
+
+    const int tid = threadIdx.x;
+    const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
+    const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
+    const int z0 = kRadius + blockIdx.z * p.chunk_z;
+    const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
+    if (z0 >= z1) return;
+    const int nzc = z1 - z0;
+    P.nplanes = nzc + 2 * kRadius;
+    P.zfirst = z0 - kRadius;
+    P.c0 = y0 - kHaloY;
+    P.c1 = x0 - kRadius;
+
+    const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml;
+    const int x = x0 + r, yq = y0 + 4 * q;
+    const bool row_ok = (r < p.tile_x) && (x < nx - kRadius);
+    bool cell_ok[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < ny - kRadius);
+    const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
+    // A quad is "interior in x,y" when all four cells are outside the x and
+    // y faces; then only the z faces can make it a PML quad.
+    const bool xy_interior = (x >= pml) && (x < nx - pml) && (yq >= pml) && (yq + 3 < ny - pml);
+    const int hy = ny - 2 * pml;
+
+    if (tid == 0) {
+        for (int s = 0; s < kRing; ++s) mbar_init(&P.bar[s], 1);
+        fence_barrier_init();
+        misc[0] = threshold_m2(*p.gmax);
+        int n = 0;
+        for (int e = 0; e < p.nsrc; ++e) {
+            SrcEntry s = p.src[e];
+            if (s.x >= x0 && s.x < x0 + p.tile_x && s.y >= y0 && s.y < y0 + kTileY && s.z >= z0 &&
+                s.z < z1 && n < kMaxFusedSources)
+                csrc[n++] = s;
+        }
+        misc_i[0] = n;
+    }
+    for (int i = tid; i < 3 * pml; i += blockDim.x) tab[i] = p.layers[i];
+    __syncthreads();
+    const float T2 = misc[0];
+    const int ncsrc = misc_i[0];
+    int issued = 0;
+    if (tid == 0) {
+        issued = min(kRing, P.nplanes);
+        for (int i = 0; i < issued; ++i) pipe_issue(P, &tm_u, i);
+    }
+
+    const Coefs &k = p.k;
+    const float dt = p.dt;
+    bool ok = true;
+    int waited = 0;
+    for (int t = 0; t < nzc; ++t) {
+        const int z = z0 + t;
+        const long long base = (long long)z * p.plane + (long long)x * p.ldy + yq;
+        // Global loads of this plane's per-cell data, issued before the wait.
+        float4 u1v = make_float4(0.f, 0.f, 0.f, 0.f), Kv = u1v, Ev = u1v, Rv = u1v;
+        if (row_ok) {
+            u1v = *reinterpret_cast<const float4 *>(p.u_io + base);
+            Kv = __ldg(reinterpret_cast<const float4 *>(p.prm_k + base));
+            Ev = __ldg(reinterpret_cast<const float4 *>(p.prm_e + base));
+            Rv = __ldg(reinterpret_cast<const float4 *>(p.prm_r + base));
+        }
+        const int need = t + 2 * kRadius;
+        while (ok && waited <= need) {
+            ok = pipe_wait(P, waited);
+            if (ok) ++waited;
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(p.err, kErrWaitTimeout);
+            break;
+        }
+        if (row_ok) {
+            float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+            quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+            float e2[4], KS[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                // scalar operator, GPU_kernel.cu:93-111
+                float h2 = __fmul_rn(Ux[j], Ux[j]);
+                h2 = fmaf(Uy[j], Uy[j], h2);
+                float m2 = fmaf(Uz[j], Uz[j], h2);
+                float s = 1.0f;
+                float e2x = f4(Ev, j);
+                if (m2 > T2) {
+                    float aa = __fdiv_rn(h2, m2);
+                    float bb = __fsub_rn(1.0f, aa);
+                    float den = fmaf(e2x, aa, 1.0f);
+                    float num = __fmul_rn(__fmul_rn(f4(Rv, j), aa), bb);
+                    float qq = __fdiv_rn(num, __fmul_rn(den, den));
+                    s = fmaf(0.5f, __fsqrt_rn(__fsub_rn(1.0f, qq)), 0.5f);
+                }
+                e2[j] = __fadd_rn(1.0f, e2x);
+                KS[j] = __fmul_rn(f4(Kv, j), s);
+            }
+            float out[4];
+            const bool interior = xy_interior && z >= pml && z < nz - pml;
+            if (interior) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
+                    out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
+                }
+            } else {
+                const float4 w11 = *reinterpret_cast<const float4 *>(p.w1o + base);
+                const float4 w12 = *reinterpret_cast<const float4 *>(p.w1c + base);
+                const float4 w31 = *reinterpret_cast<const float4 *>(p.w3o + base);
+                const float4 w32 = *reinterpret_cast<const float4 *>(p.w3c + base);
+                const float4 p1 = *reinterpret_cast<const float4 *>(p.po + base);
+                const float4 p2 = *reinterpret_cast<const float4 *>(p.pc + base);
+                const float4 w21 = *reinterpret_cast<const float4 *>(p.w21 + base);
+                float n13[4], n21[4], n33[4], n3[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int y = yq + j;
+                    const int f = cell_ok[j] ? region_of(x, y, z, nx, ny, nz, pml) : -2;
+                    n13[j] = 0.0f; n33[j] = 0.0f; n3[j] = 0.0f; n21[j] = f4(w21, j);
+                    if (f == -2) {
+                        out[j] = f4(u1v, j);   // outside [5,n-5)^3: never updated
+                    } else if (f < 0) {
+                        float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
+                        out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
+                    } else {
+                        int li, pr;
+                        switch (f) {
+                        case F_L: li = pml - x; pr = 0; break;
+                        case F_R: li = x - nx + pml; pr = 0; break;
+                        case F_F: li = pml - y; pr = 1; break;
+                        case F_BK: li = y - ny + pml; pr = 1; break;
+                        case F_T: li = pml - z; pr = 2; break;
+                        default: li = z - nz + pml; pr = 2; break;
+                        }
+                        out[j] = pml_cell(f, tab[pr * pml + li], KS[j], e2[j], Ux[j], Uy[j], Uz[j],
+                                          Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
+                                          f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
+                                          n13[j], n21[j], n33[j], n3[j]);
+                    }
+                }
+                *reinterpret_cast<float4 *>(p.w1n + base) = make_float4(n13[0], n13[1], n13[2], n13[3]);
+                *reinterpret_cast<float4 *>(p.w3n + base) = make_float4(n33[0], n33[1], n33[2], n33[3]);
+                *reinterpret_cast<float4 *>(p.pn + base) = make_float4(n3[0], n3[1], n3[2], n3[3]);
+                *reinterpret_cast<float4 *>(p.w21 + base) = make_float4(n21[0], n21[1], n21[2], n21[3]);
+            }
+            // source injection (GPU_kernel.cu:727): u3 += source * wavelet
+            for (int e = 0; e < ncsrc; ++e) {
+                const SrcEntry s = csrc[e];
+                if (s.z == z && s.x == x) {
+                    int j = s.y - yq;
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj)
+                        if (jj == j) out[jj] = __fadd_rn(out[jj], __fmul_rn(s.v, p.wavelet));
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (!cell_ok[j]) out[j] = f4(u1v, j);
+            *reinterpret_cast<float4 *>(p.u_io + base) = make_float4(out[0], out[1], out[2], out[3]);
+            // receiver plane (3dPureqPModeling_single_shot.cu:333-337)
+            if (p.record && z == p.sz && x >= pml && x < nx - pml) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int y = yq + j;
+                    if (cell_ok[j] && y >= pml && y < ny - pml)
+                        p.record[(long long)(x - pml) * hy + (y - pml)] = out[j];
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && t + kRing < P.nplanes) {
+            fence_proxy_async();
+            pipe_issue(P, &tm_u, t + kRing);
+            issued = t + kRing + 1;
+        }
+    }
+    if (!ok && tid == 0) pipe_drain(P, waited, issued);
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels
+// ---------------------------------------------------------------------------
+
+// Sources outside the updated box [5,n-5)^3: the reference never updates
+// those cells, so u3 there is its previous value plus the source
+// (CPU_function.c:326-338 on a cell wavefield_update skips); with two
+// buffers that previous value is u(k).
+__global__ void qp3d_band_source_kernel(float *u_new, const float *u_cur, const SrcEntry *src,
+                                        int n, long long plane, int ldy, float w)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    SrcEntry s = src[e];
+    long long i = (long long)s.z * plane + (long long)s.x * ldy + s.y;
+    u_new[i] = __fadd_rn(u_cur[i], __fmul_rn(s.v, w));
+}
+
+// All sources, after the step kernel (used when there are too many to fuse).
+__global__ void qp3d_all_source_kernel(float *u_new, const float *u_cur, const SrcEntry *src,
+                                       int n, long long plane, int ldy, int nx, int ny, int nz,
+                                       float w)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    SrcEntry s = src[e];
+    long long i = (long long)s.z * plane + (long long)s.x * ldy + s.y;
+    bool inside = s.x >= kRadius && s.x < nx - kRadius && s.y >= kRadius && s.y < ny - kRadius &&
+                  s.z >= kRadius && s.z < nz - kRadius;
+    float prev = inside ? u_new[i] : u_cur[i];
+    u_new[i] = __fadd_rn(prev, __fmul_rn(s.v, w));
+}
+
+__global__ void qp3d_record_kernel(const float *u, float *rec, int nx, int ny, int pml, int sz,
+                                   int ldy, long long plane)
+{
+    int hx = nx - 2 * pml, hy = ny - 2 * pml;
+    long long n = (long long)hx * hy;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        int xi = (int)(i / hy), yi = (int)(i % hy);
+        rec[i] = u[(long long)sz * plane + (long long)(xi + pml) * ldy + yi + pml];
+    }
+}
+
+__global__ void qp3d_crop_kernel(const float *u, float *out, int x0, int x1, int y0, int y1,
+                                 int z0, int z1, int ldy, long long plane)
+{
+    long long nyc = y1 - y0, nxc = x1 - x0, nzc = z1 - z0;
+    long long n = nxc * nyc * nzc;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long yi = i % nyc, xi = (i / nyc) % nxc, zi = i / (nyc * nxc);
+        out[i] = u[(zi + z0) * plane + (xi + x0) * ldy + yi + y0];
+    }
+}
+
+// Per-cell parameters from vp, eps, delta (in place: K holds vp, E2 holds
+// eps, R8 holds delta on entry).
+__global__ void qp3d_params_kernel(float *K, float *E2, float *R8, long long n, float dt)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float vdt = __fmul_rn(K[i], dt);
+        float e = E2[i], d = R8[i];
+        K[i] = __fmul_rn(vdt, vdt);
+        E2[i] = __fmul_rn(2.0f, e);
+        R8[i] = __fmul_rn(8.0f, __fsub_rn(e, d));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+cudaError_t configure_kernels()
+{
+    cudaError_t e = cudaFuncSetAttribute(qp3d_step_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(qp3d_gradmax_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                200 * 1024);
+}
+
+cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
+                           cudaStream_t stream)
+{
+    qp3d_gradmax_kernel<<<grid, kQuadsY * p.tile_x, smem, stream>>>(tm_u, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
+                        cudaStream_t stream)
+{
+    qp3d_step_kernel<<<grid, kQuadsY * p.tile_x, smem, stream>>>(tm_u, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_band_sources(float *u_new, const float *u_cur, const SrcEntry *src, int n,
+                                long long plane, int ldy, float w, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    qp3d_band_source_kernel<<<(n + 127) / 128, 128, 0, stream>>>(u_new, u_cur, src, n, plane, ldy,
+                                                                 w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_all_sources(float *u_new, const float *u_cur, const SrcEntry *src, int n,
+                               long long plane, int ldy, int nx, int ny, int nz, float w,
+                               cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    qp3d_all_source_kernel<<<(n + 255) / 256, 256, 0, stream>>>(u_new, u_cur, src, n, plane, ldy,
+                                                                nx, ny, nz, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_record(const float *u, float *rec, int nx, int ny, int pml, int sz, int ldy,
+                          long long plane, cudaStream_t stream)
+{
+    long long n = (long long)(nx - 2 * pml) * (ny - 2 * pml);
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    if (blocks < 1) blocks = 1;
+    qp3d_record_kernel<<<blocks, 256, 0, stream>>>(u, rec, nx, ny, pml, sz, ldy, plane);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0, int y1, int z0, int z1,
+                        int ldy, long long plane, cudaStream_t stream)
+{
+    long long n = (long long)(x1 - x0) * (y1 - y0) * (z1 - z0);
+    if (n <= 0) return cudaSuccess;
+    long long b = (n + 255) / 256;
+    int blocks = (int)(b > 8192 ? 8192 : b);
+    qp3d_crop_kernel<<<blocks, 256, 0, stream>>>(u, out, x0, x1, y0, y1, z0, z1, ldy, plane);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_params(const float * /*vp*/, const float * /*eps*/, const float * /*del*/,
+                          float *K, float *E2, float *R8, long long n, float dt,
+                          cudaStream_t stream)
+{
+    long long b = (n + 255) / 256;
+    int blocks = (int)(b > 8192 ? 8192 : b);
+    qp3d_params_kernel<<<blocks, 256, 0, stream>>>(K, E2, R8, n, dt);
+    return cudaGetLastError();
+}
+
+}  // namespace qp3d

@@ -1,0 +1,94 @@
+"""Seeded synthetic shots for the workloads the library is measured on.
+
+There is no field data here, so each workload is a generated earth model with
+the sizes, spacings and parameter ranges of the published configurations.
+Inputs are built exactly as the reference's main program builds them
+(3dPureqPModeling1.0.c:234-268): interior model -> extend_model into the PML
+shell -> vpmax = (1 + 2 max eps) max vp -> pmlcoff -> Source at the window
+centre on the top of the interior, receivers on that plane.
+"""
+import numpy as np
+
+import qp3d
+
+
+def _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=None, sz=None, amp=1.0,
+            alpha=1.0):
+    nz0, hx, hy = vp_i.shape
+    nx, ny, nz = hx + 2 * pml, hy + 2 * pml, nz0 + 2 * pml
+    vp = qp3d.extend_model(vp_i, nx, ny, nz, pml)
+    eps = qp3d.extend_model(eps_i, nx, ny, nz, pml)
+    dl = qp3d.extend_model(del_i, nx, ny, nz, pml)
+    vpmax = np.float32((1 + 2 * qp3d.absmax(eps)) * qp3d.absmax(vp))
+    prof = qp3d.pmlcoff(pml, float(vpmax), dx, dx, dx)
+    if src_xyz is None:   # 3dPureqPModeling1.0.c:263-265
+        src_xyz = ((hx - 1) // 2, (hy - 1) // 2, 0)
+    sx, sy, sz0 = (v + pml for v in src_xyz)
+    src, wav = qp3d.source(sx, sy, sz0, fm, amp, alpha, dt, dx, dx, dx, 1.0 / fm, nt,
+                           nx, ny, nz)
+    c, c2 = qp3d.fdcoff()
+    if sz is None:
+        sz = sz0
+    return qp3d.Shot(nx, ny, nz, pml, sz, dx, dx, dx, dt, vp, eps, dl, src, wav, prof, c, c2)
+
+
+def linear_vti(h=100, nz0=100, pml=20, nt=1000, dx=10.0, dt=5e-4, fm=25.0, src=(50, 50, 5),
+               vp_top=2000.0, vp_bottom=3500.0, eps=0.2, delta=0.1):
+    """Plain single-shot workload: vp linear in depth, uniform eps/delta,
+    point source at `src` (interior cells), receivers on the source plane.
+    Defaults: 100^3 interior, 20-cell PML, 1000 steps of 0.5 ms, 25 Hz."""
+    z = np.arange(nz0, dtype=np.float64)
+    vpz = (vp_top + (vp_bottom - vp_top) * z / max(nz0 - 1, 1)).astype(np.float32)
+    vp_i = np.broadcast_to(vpz[:, None, None], (nz0, h, h)).astype(np.float32)
+    eps_i = np.full((nz0, h, h), eps, np.float32)
+    del_i = np.full((nz0, h, h), delta, np.float32)
+    return _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=src)
+
+
+def layered_vti(hx=400, hy=400, nz0=300, pml=30, nt=3000, dx=10.0, dt=5e-4, fm=20.0,
+                nlayers=12, seed=2, slope=0.15, src=None):
+    """Layered model with dipping planar interfaces: per layer vp U[1500,4500],
+    eps U[0,0.3], delta U[0,min(eps,0.15)].  Defaults: 400x400x300 interior,
+    30-cell PML, 3000 steps, 20 Hz source at the surface centre."""
+    rng = np.random.default_rng(seed)
+    z0 = np.sort(rng.uniform(0, nz0, nlayers - 1))
+    ax = rng.uniform(-slope, slope, nlayers - 1)
+    ay = rng.uniform(-slope, slope, nlayers - 1)
+    lvp = rng.uniform(1500, 4500, nlayers).astype(np.float32)
+    leps = rng.uniform(0, 0.3, nlayers).astype(np.float32)
+    ldel = np.array([rng.uniform(0, min(e, 0.15)) for e in leps], np.float32)
+    xs = np.arange(hx, dtype=np.float64)[:, None] - hx / 2
+    ys = np.arange(hy, dtype=np.float64)[None, :] - hy / 2
+    idx = np.zeros((nz0, hx, hy), np.int8)
+    zz = np.arange(nz0, dtype=np.float64)[:, None, None]
+    for i in range(nlayers - 1):
+        depth = z0[i] + ax[i] * xs + ay[i] * ys
+        idx += (zz >= depth[None]).astype(np.int8)
+    vp_i, eps_i, del_i = lvp[idx], leps[idx], ldel[idx]
+    return _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=src)
+
+
+def small_case(hx=22, hy=26, nz0=18, pml=8, nt=60, seed=7, fm=30.0, src=None, dt=5e-4):
+    """Small non-cubic layered case for fast parity tests (every PML face and
+    corner is reached within a few tens of steps)."""
+    if src is None:
+        src = (hx // 2, hy // 3, nz0 // 3)
+    return layered_vti(hx=hx, hy=hy, nz0=nz0, pml=pml, nt=nt, dt=dt, fm=fm, nlayers=4,
+                       seed=seed, slope=0.3, src=src)
+
+
+def random_state(shot, seed=0, amp=1e-3):
+    """Random u(k-1), u(k) and PML state (reference face layout), non-zero on
+    every cell the reference updates, for single-step operator tests."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz, pml = shot.nx, shot.ny, shot.nz, shot.pml
+    def vol():
+        v = np.zeros((nz, nx, ny), np.float32)
+        # smooth-ish random field so that gradients straddle the threshold
+        v[5:-5, 5:-5, 5:-5] = (amp * rng.standard_normal((nz - 10, nx - 10, ny - 10))).astype(
+            np.float32)
+        return v.ravel()
+    u_prev, u_cur = vol(), vol()
+    n = qp3d.pml_state_size(nx, ny, nz, pml)
+    pml_state = (amp * rng.standard_normal(n + 1)).astype(np.float32)
+    return u_prev, u_cur, pml_state

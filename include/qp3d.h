@@ -1,0 +1,159 @@
+/*
+ * qp3d.h -- C ABI of the GB300 implementation of the 3D pure-qP VTI
+ * finite-difference modeling loop of hlc0216/Gpu-c_3dqmodeling.
+ *
+ * Plain C: pointers and sizes only.  All host pointers are caller-owned; the
+ * library owns every device buffer (one reusable context per device and
+ * host thread).  Every entry point returns QP3D_OK (0) or a negative code;
+ * nothing calls exit().
+ *
+ * Grid convention (as the reference, array_new.c:2 and Main.c:125): padded
+ * sizes nx = hx + 2*pml, ny = hy + 2*pml, nz = Nz0 + 2*pml; volumes are
+ * [nz][nx][ny] float32 with y fastest.  The record is [nt][hx][hy].
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   qp3d_forward ............ modeling3d, 3dPureqPModeling_single_shot.h:4-6
+ *                             (GPU impl 3dPureqPModeling_single_shot.cu:26-447,
+ *                             CPU impl modeling3D.c:17-153)
+ *   qp3d_shot_* ............. the same call split into load / advance / read
+ *                             so that callers can keep the model resident
+ *   qp3d_fdcoff1/2 .......... fdcoff1/fdcoff2, CPU_function.c:111-148
+ *   qp3d_pmlcoff ............ pmlcoff, CPU_function.c:150-169
+ *   qp3d_source ............. Source, CPU_function.c:37-64
+ *   qp3d_extend_model ....... extend_model, CPU_function.c:67-108
+ *   qp3d_readmodel3d ........ readmodel3d, CPU_function.c:234-261
+ *   qp3d_absmax ............. absMaxval, CPU_function.c:10-22
+ * The C++-linkage symbol modeling3d itself is declared in qp3d_modeling3d.h.
+ */
+#ifndef QP3D_H
+#define QP3D_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QP3D_OK 0
+#define QP3D_ERR_ARG (-1)       /* invalid argument or geometry */
+#define QP3D_ERR_CUDA (-2)      /* CUDA runtime/driver error */
+#define QP3D_ERR_NOMEM (-3)     /* device or host allocation failed */
+#define QP3D_ERR_TIMEOUT (-4)   /* a bounded device wait expired */
+#define QP3D_ERR_STATE (-5)     /* call out of order (no shot loaded, ...) */
+#define QP3D_ERR_IO (-6)        /* file could not be read or written */
+#define QP3D_ERR_CALLBACK (-7)  /* a snapshot callback returned non-zero */
+
+typedef struct qp3d_ctx qp3d_ctx;
+
+typedef struct {
+    int nx, ny, nz;   /* padded grid (cells) */
+    int nt;           /* time steps */
+    int pml;          /* absorbing layer thickness (cells) */
+    int sz;           /* receiver depth, padded z index */
+    float dx, dy, dz; /* spacing (m) */
+    float dt;         /* time step (s) */
+} qp3d_geom;
+
+typedef struct {
+    const float *vp, *epsilon, *delta;   /* padded volumes */
+    const float *source;                 /* padded source volume, or NULL */
+    const float *wavelet;                /* nt amplitudes */
+    const float *dlr, *ddlr;             /* x-face damping profiles, pml each */
+    const float *dtb, *ddtb;             /* z-face */
+    const float *dfb, *ddfb;             /* y-face */
+    const float *c, *c2;                 /* 36-entry tables of fdcoff1/fdcoff2 */
+} qp3d_model;
+
+/* Snapshots (3dPureqPModeling_single_shot.cu:340-377): every ntsnap steps,
+ * after the step, the interior wavefield and/or its mid slices. */
+enum {
+    QP3D_SNAP_VOLUME = 0,   /* [Nz0][hx][hy] */
+    QP3D_SNAP_XZ = 1,       /* [Nz0][hx] at y = (hy-1)/2 */
+    QP3D_SNAP_YZ = 2,       /* [Nz0][hy] at x = (hx-1)/2 */
+    QP3D_SNAP_XY = 3        /* [hx][hy]  at z = (Nz0-1)/2 */
+};
+typedef int (*qp3d_snap_fn)(void *user, int step, int kind, const float *data,
+                            int n0, int n1, int n2);
+typedef struct {
+    int ntsnap;             /* 0: no snapshots */
+    unsigned kinds;         /* bit mask of (1u << QP3D_SNAP_*) */
+    qp3d_snap_fn fn;
+    void *user;
+} qp3d_snap;
+
+int qp3d_version(void);
+const char *qp3d_strerror(int code);
+
+/* Context: binds a device and a stream.  Not thread-safe per context. */
+int qp3d_ctx_create(int device, qp3d_ctx **out);
+void qp3d_ctx_destroy(qp3d_ctx *ctx);
+const char *qp3d_ctx_last_error(const qp3d_ctx *ctx);
+
+/* One shot, host buffers in and out: the replacement of modeling3d.
+ * record: caller-allocated nt*hx*hy floats, fully overwritten.
+ * snap: NULL for none. */
+int qp3d_forward(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m,
+                 float *record, const qp3d_snap *snap);
+
+/* Staged form of the same shot. */
+int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m);
+int qp3d_shot_reset(qp3d_ctx *ctx);                 /* zero state, step 0 */
+int qp3d_shot_advance(qp3d_ctx *ctx, int nsteps);   /* enqueue, asynchronous */
+int qp3d_shot_sync(qp3d_ctx *ctx);                  /* wait, check errors */
+int qp3d_shot_step(const qp3d_ctx *ctx);            /* steps done */
+int qp3d_shot_read_record(qp3d_ctx *ctx, int k0, int nsteps, float *out);
+int qp3d_shot_read_uxyzmax(qp3d_ctx *ctx, int k0, int nsteps, float *out);
+/* Snapshot of the current step through the same callback as qp3d_forward. */
+int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap);
+
+/* Full state in the reference's own layout (test and checkpoint use):
+ * u_prev = u(k-1), u_cur = u(k) as padded volumes; pml_state as six faces
+ * L,R,F,B,T,Bo (GPU_kernel.cu:568-628 indexing), each ten arrays
+ * w11,w12,w13,w21,w31,w32,w33,p1,p2,p3; only w11,w12,w21,w31,w32,p1,p2 are
+ * live between steps.  NULL pointers are skipped. */
+size_t qp3d_pml_state_size(int nx, int ny, int nz, int pml);
+int qp3d_shot_write_state(qp3d_ctx *ctx, int step, const float *u_prev,
+                          const float *u_cur, const float *pml_state);
+int qp3d_shot_read_state(qp3d_ctx *ctx, float *u_prev, float *u_cur,
+                         float *pml_state);
+
+/* Device timing of nsteps further steps with CUDA events on the context's
+ * stream.  ms_total: whole interval; ms_step / ms_gradmax: sums of the
+ * per-launch durations of the two kernels (NULL to skip per-kernel events). */
+int qp3d_shot_time(qp3d_ctx *ctx, int nsteps, float *ms_total, float *ms_step,
+                   float *ms_gradmax);
+/* Number of kernels the library launches per time step for the loaded shot. */
+int qp3d_shot_launches_per_step(const qp3d_ctx *ctx);
+
+/* CUDA events on the context's stream, for timing any sequence of library
+ * calls on the stream the kernels run on.  slot in [0, 8). */
+int qp3d_event_record(qp3d_ctx *ctx, int slot);
+int qp3d_event_elapsed(qp3d_ctx *ctx, int slot_start, int slot_end, float *ms);
+
+/* Page-locked host memory (cudaMallocHost), for inputs and records that
+ * cross the host link at full speed.  NULL on failure. */
+void *qp3d_host_alloc(size_t bytes);
+void qp3d_host_free(void *p);
+
+/* Host utilities, restating the reference's (see the list above). */
+void qp3d_fdcoff1(float *c);
+void qp3d_fdcoff2(float *c2);
+void qp3d_pmlcoff(int pml, float vpmax, float dx, float dy, float dz,
+                  float *dlr, float *ddlr, float *dtb, float *ddtb,
+                  float *dfb, float *ddfb);
+void qp3d_source(int sx, int sy, int sz, float fm, float amp, float alpha,
+                 float dt, float dx, float dy, float dz, float t0, int nt,
+                 int nx, int ny, int nz, float *source, float *wavelet);
+void qp3d_extend_model(const float *in, float *out, int nx, int ny, int nz,
+                       int pml);
+float qp3d_absmax(const float *a, size_t n);
+/* Window [fny,fny+ny) x [fnx,fnx+nx) x [fnz,fnz+nz) of a file stored
+ * [vny][vnx][vnz] (z fastest) into a[nz][nx][ny].  Unlike the reference it
+ * fails with QP3D_ERR_IO on a missing file or a short read. */
+int qp3d_readmodel3d(const char *filename, float *a, int ny, int nx, int nz,
+                     int fny, int fnx, int fnz, int vny, int vnx, int vnz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QP3D_H */

@@ -1,0 +1,71 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+* ``oracle/lib/libqp3d_oracle.so`` -- the C restatement in qp3d_oracle.c
+  (FP32 reference arithmetic, FP64, and the kernel-arithmetic mirror).
+* ``oracle/_ref/libqp3d_ref.so`` -- the reference's own CPU_function.c compiled
+  in place from the reference checkout plus ref_harness.cpp.  Built only where
+  that checkout exists; its path comes from QP3D_REFERENCE_DIR (default
+  ``/root/reference``).  Nothing is copied out of the checkout; the output
+  directory is git-ignored.
+
+Both are built with ``-ffp-contract=off`` so that no compiler fuses a*b+c and
+the FP32 roundings are the ones written in the source, on x86 and on Arm.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "libqp3d_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libqp3d_ref.so")
+REFERENCE_DIR = os.environ.get("QP3D_REFERENCE_DIR", "/root/reference")
+
+COMMON = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp"]
+
+
+def _newer(target, sources):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "qp3d_oracle.c")
+    hdr = os.path.join(HERE, "qp3d_oracle.h")
+    if force or _newer(LIB, [src, hdr]):
+        os.makedirs(os.path.dirname(LIB), exist_ok=True)
+        cmd = ["gcc", "-std=c11", "-Wall"] + COMMON + ["-o", LIB, src, "-lm"]
+        subprocess.check_call(cmd)
+    return LIB
+
+
+def reference_available():
+    return os.path.isfile(os.path.join(REFERENCE_DIR, "CPU_function.c"))
+
+
+def build_reference(force=False):
+    """Compile the reference CPU operators; returns the .so path or None."""
+    if not reference_available():
+        return None
+    ref_src = os.path.join(REFERENCE_DIR, "CPU_function.c")
+    harness = os.path.join(HERE, "ref_harness.cpp")
+    if force or _newer(REF_LIB, [ref_src, harness]):
+        os.makedirs(os.path.dirname(REF_LIB), exist_ok=True)
+        # The reference builds its .c files with g++ (Makefile:9), i.e. as C++.
+        cmd = (["g++", "-x", "c++", "-w"] + COMMON +
+               ["-Dexchange=qp3d_ref_exchange_unused", "-I", REFERENCE_DIR,
+                "-o", REF_LIB, ref_src, harness, "-lm"])
+        subprocess.check_call(cmd)
+    return REF_LIB
+
+
+def build(force=False):
+    build_oracle(force)
+    build_reference(force)
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv)
+    print(LIB)
+    print(REF_LIB if os.path.exists(REF_LIB) else "(reference not built)")

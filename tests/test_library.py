@@ -1,0 +1,134 @@
+"""libqp3d.so host-side checks that need no GPU.
+
+The library must load without a GPU driver, export every symbol the public
+headers declare, and its host utilities must reproduce the reference's
+(CPU_function.c) bit for bit -- checked against the oracle, which is pinned
+to the reference by test_oracle.py.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import qp3d
+from oracle import oracle as O
+from helpers import bits_equal, load_fixture
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    for h in ("qp3d.h",):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(qp3d_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_exports_every_declared_symbol():
+    lib = qp3d.load()
+    declared = _declared_symbols()
+    assert declared, "no declarations parsed"
+    assert declared <= set(qp3d.EXPORTS), declared - set(qp3d.EXPORTS)
+    for name in declared:
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", qp3d.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    assert re.search(r"\bT _Z10modeling3d", out), "C++-linkage modeling3d drop-in missing"
+
+
+def test_no_runtime_dependency_on_cuda_driver():
+    out = subprocess.run(["ldd", qp3d.LIB_PATH], capture_output=True, text=True).stdout
+    assert "libcuda.so" not in out and "libcudart.so" not in out
+
+
+def test_fdcoff_matches_oracle():
+    c, c2 = qp3d.fdcoff()
+    oc, oc2 = O.fdcoff()
+    assert bits_equal(c, oc) and bits_equal(c2, oc2)
+
+
+@pytest.mark.parametrize("pml,vpmax,dx,dy,dz", [(20, 4900.0, 10.0, 10.0, 10.0),
+                                                (30, 6300.0, 12.5, 10.0, 8.0), (5, 3000.0, 5.0, 5.0, 5.0)])
+def test_pmlcoff_matches_oracle(pml, vpmax, dx, dy, dz):
+    a = qp3d.pmlcoff(pml, vpmax, dx, dy, dz)
+    b = O.pmlcoff(pml, vpmax, dx, dy, dz)
+    for x, y in zip(a, b):
+        assert bits_equal(x, y)
+
+
+@pytest.mark.parametrize("alpha", [1.0, 0.05])
+def test_source_matches_oracle(alpha):
+    args = (9, 11, 7, 25.0, 1.0, alpha, 5e-4, 10.0, 10.0, 10.0, 1.0 / 25.0, 300, 21, 23, 19)
+    s1, w1 = qp3d.source(*args)
+    s2, w2 = O.source(*args)
+    assert bits_equal(s1, s2)
+    assert bits_equal(w1, w2)
+
+
+def test_extend_model_matches_oracle():
+    rng = np.random.default_rng(3)
+    interior = rng.standard_normal((9, 13, 11)).astype(np.float32)
+    pml = 6
+    a = qp3d.extend_model(interior, 13 + 2 * pml, 11 + 2 * pml, 9 + 2 * pml, pml)
+    b = O.extend_model(interior, 13 + 2 * pml, 11 + 2 * pml, 9 + 2 * pml, pml)
+    assert bits_equal(a, b)
+
+
+def test_absmax_semantics():
+    a = np.array([0.0, -3.0, 2.0, np.nan, -3.0], np.float32)
+    assert qp3d.absmax(a) == 3.0
+    assert qp3d.absmax(np.zeros(4, np.float32)) == 0.0
+
+
+def test_readmodel3d_window(tmp_path):
+    """File [vny][vnx][vnz] (z fastest, model/grey3_tmp.rsf) -> a[nz][nx][ny]."""
+    vny, vnx, vnz = 7, 6, 5
+    data = np.arange(vny * vnx * vnz, dtype=np.float32).reshape(vny, vnx, vnz)
+    f = tmp_path / "m.dat"
+    data.tofile(f)
+    ny, nx, nz, fny, fnx, fnz = 3, 4, 2, 2, 1, 3
+    out = np.zeros(nz * nx * ny, np.float32)
+    rc = qp3d.load().qp3d_readmodel3d(str(f).encode(), out.ctypes.data_as(ctypes.c_void_p),
+                                      ny, nx, nz, fny, fnx, fnz, vny, vnx, vnz)
+    assert rc == 0
+    want = data[fny:fny + ny, fnx:fnx + nx, fnz:fnz + nz].transpose(2, 1, 0)
+    assert np.array_equal(out.reshape(nz, nx, ny), want)
+    # missing file and a window past the end are errors, not silent garbage
+    assert qp3d.load().qp3d_readmodel3d(str(tmp_path / "nope.dat").encode(),
+                                        out.ctypes.data_as(ctypes.c_void_p),
+                                        ny, nx, nz, 0, 0, 0, vny, vnx, vnz) == -6
+    assert qp3d.load().qp3d_readmodel3d(str(f).encode(), out.ctypes.data_as(ctypes.c_void_p),
+                                        ny, nx, nz, 5, 0, 0, vny, vnx, vnz) == -1
+
+
+def test_pml_state_size_matches_oracle():
+    for g in [(40, 44, 38, 10), (140, 140, 140, 20), (31, 37, 29, 0)]:
+        assert qp3d.pml_state_size(*g) == O.pml_state_size(*g)
+
+
+def test_synthetic_generators_are_deterministic():
+    import synthetic
+    a = synthetic.small_case(seed=5)
+    b = synthetic.small_case(seed=5)
+    assert bits_equal(a.vp, b.vp) and bits_equal(a.eps, b.eps) and bits_equal(a.src, b.src)
+    c = synthetic.small_case(seed=6)
+    assert not bits_equal(a.vp, c.vp)
+    assert a.nt == 60 and a.nx == 22 + 16
+
+
+def test_context_without_device_fails_cleanly():
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = os.path.exists("/dev/nvidia0")
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(qp3d.QP3DError):
+        qp3d.Context(0)
