@@ -259,10 +259,15 @@ class Context:
     def forward(self, shot, snap=None, record=None):
         if record is None:
             record = np.empty((shot.nt, shot.hx, shot.hy), np.float32)
+        if record.size != shot.nt * shot.hx * shot.hy or record.dtype != np.float32 or \
+                not record.flags.c_contiguous:
+            raise ValueError("record must be a contiguous float32 array of nt*hx*hy")
         g, m = shot.geom(), shot.model()
         sp = ctypes.byref(snap) if snap is not None else None
+        self._shot = None
         self._check(self._L.qp3d_forward(self.h, ctypes.byref(g), ctypes.byref(m),
                                          _p(record), sp), "qp3d_forward")
+        self._shot = shot
         return record
 
     def load(self, shot, nt=None):
@@ -285,7 +290,7 @@ class Context:
         return int(self._L.qp3d_shot_step(self.h))
 
     def record(self, k0=0, n=None):
-        s = self._shot
+        s = self._loaded()
         if n is None:
             n = self.step - k0
         out = np.empty((n, s.hx, s.hy), np.float32)
@@ -305,8 +310,13 @@ class Context:
         self._check(self._L.qp3d_shot_write_state(self.h, step, _p(u_prev), _p(u_cur), _p(pml)),
                     "write_state")
 
+    def _loaded(self):
+        if self._shot is None:
+            raise QP3DError("no shot loaded through this binding")
+        return self._shot
+
     def read_state(self):
-        s = self._shot
+        s = self._loaded()
         u_prev = np.empty(s.N, np.float32)
         u_cur = np.empty(s.N, np.float32)
         pml = np.empty(pml_state_size(s.nx, s.ny, s.nz, s.pml) + 1, np.float32)
