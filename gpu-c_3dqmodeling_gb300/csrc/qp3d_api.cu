@@ -67,6 +67,8 @@ struct qp3d_ctx {
     size_t snap_cap = 0;
     cudaEvent_t ev[4] = {};
     cudaEvent_t uev[8] = {};
+    // tuning
+    int step_variant = 1, gradmax_variant = 1, tune_tile_x = 0, tune_chunks = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -221,6 +223,7 @@ static void plan_launch(qp3d_ctx *ctx)
     int ncx = g.nx - 2 * kRadius;
     int ntx = (ncx + kMaxTileX - 1) / kMaxTileX;
     ctx->tile_x = (ncx + ntx - 1) / ntx;
+    if (ctx->tune_tile_x > 0) ctx->tile_x = std::min(ctx->tune_tile_x, kMaxTileX);
     ctx->nxt = (ncx + ctx->tile_x - 1) / ctx->tile_x;
     ctx->nyt = (g.ny - kRadius - 1) / kTileY + 1;   // last tile starts below ny-5
     int ncz = g.nz - 2 * kRadius;
@@ -229,6 +232,7 @@ static void plan_launch(qp3d_ctx *ctx)
     int nch = (int)((target + tiles - 1) / tiles);
     int maxch = std::max(1, ncz / 24);
     nch = std::max(1, std::min(nch, maxch));
+    if (ctx->tune_chunks > 0) nch = std::min(ctx->tune_chunks, ncz);
     ctx->chunk_z = (ncz + nch - 1) / nch;
     ctx->nchunks = (ncz + ctx->chunk_z - 1) / ctx->chunk_z;
     ctx->smem = plane_smem_bytes(ctx->tile_x, g.pml);
@@ -411,10 +415,10 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     dim3 grid(ctx->nyt, ctx->nxt, ctx->nchunks);
 
     if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
-    CK(launch_gradmax(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
+    CK(launch_gradmax(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->gradmax_variant));
     if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
     if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
-    CK(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
+    CK(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->step_variant));
     if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
     if (ctx->fuse_sources) {
         CK(launch_band_sources(ctx->U[b], ctx->U[a], ctx->src_band, ctx->n_band, ctx->plane,
@@ -776,4 +780,33 @@ extern "C" void *qp3d_host_alloc(size_t bytes)
 extern "C" void qp3d_host_free(void *p)
 {
     if (p) cudaFreeHost(p);
+}
+
+extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
+{
+    if (!ctx || !key) return QP3D_ERR_ARG;
+    if (!strcmp(key, "step_variant") && (value == 0 || value == 1)) ctx->step_variant = value;
+    else if (!strcmp(key, "gradmax_variant") && (value == 0 || value == 1)) ctx->gradmax_variant = value;
+    else if (!strcmp(key, "tile_x") && value >= 0 && value <= kMaxTileX) ctx->tune_tile_x = value;
+    else if (!strcmp(key, "chunks") && value >= 0) ctx->tune_chunks = value;
+    else return fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
+    if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaStreamSynchronize(ctx->stream));
+        plan_launch(ctx);
+        int rc;
+        if ((rc = make_tmap(ctx, ctx->U[0], &ctx->tm[0])) || (rc = make_tmap(ctx, ctx->U[1], &ctx->tm[1])))
+            return rc;
+    }
+    return QP3D_OK;
+}
+
+extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
+{
+    if (!ctx || !key) return QP3D_ERR_ARG;
+    if (!strcmp(key, "step_variant")) return ctx->step_variant;
+    if (!strcmp(key, "gradmax_variant")) return ctx->gradmax_variant;
+    if (!strcmp(key, "tile_x")) return ctx->loaded ? ctx->tile_x : ctx->tune_tile_x;
+    if (!strcmp(key, "chunks")) return ctx->loaded ? ctx->nchunks : ctx->tune_chunks;
+    return QP3D_ERR_ARG;
 }

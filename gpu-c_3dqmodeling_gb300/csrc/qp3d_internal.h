@@ -78,9 +78,9 @@ struct Shot;   // host-side, defined in qp3d_api.cu
 // Launchers (qp3d_kernels.cu).  All enqueue on `stream` and return the
 // launch error.
 cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p,
-                           dim3 grid, size_t smem, cudaStream_t stream);
+                           dim3 grid, size_t smem, cudaStream_t stream, int variant);
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p,
-                        dim3 grid, size_t smem, cudaStream_t stream);
+                        dim3 grid, size_t smem, cudaStream_t stream, int variant);
 cudaError_t launch_band_sources(float *u_new, const float *u_cur,
                                 const SrcEntry *src, int n, long long plane,
                                 int ldy, float w, cudaStream_t stream);

@@ -140,7 +140,7 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_x, int pml)
     L.slot_floats = (box + 31) & ~(size_t)31;
     L.ring_bytes = L.slot_floats * 4 * kRing;
     L.bar_off = L.ring_bytes;
-    L.tab_off = L.bar_off + 8 * kRing;
+    L.tab_off = L.bar_off + 16 * kRing;   // full[kRing], empty[kRing]
     L.tab_off = (L.tab_off + 15) & ~(size_t)15;
     L.src_off = L.tab_off + 16 * 3 * (size_t)(pml > 0 ? pml : 1);
     L.misc_off = L.src_off + sizeof(SrcEntry) * kMaxFusedSources;
@@ -264,52 +264,114 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
 }
 
 // ---------------------------------------------------------------------------
-// Common pipeline: prologue (barriers, first loads) and the per-plane wait /
-// refill.  Returns false when a wait timed out (error bit set).
+// Plane pipeline.  Staged plane i of a chunk holds z = zfirst + i, in slot
+// s = i % kRing.  full[s] completes when the TMA load of a plane into s has
+// landed (one arrival + transaction bytes); empty[s] completes when every
+// consumer warp has finished with the plane in s.  Plane i is last read by
+// iteration t = i (as the z-5 tap of plane z = zfirst + i + 5), so warps
+// release slot t % kRing after iteration t and thread 0 refills it with plane
+// t + kRing.  No CTA-wide barrier in the plane loop.
 // ---------------------------------------------------------------------------
 struct Pipe {
     float *ring;
-    uint64_t *bar;
+    uint64_t *full, *empty;
     size_t slot_floats;
     unsigned box_bytes;
     int nplanes;     // planes to stage for this chunk
     int zfirst;      // z of staged plane 0
     int c0, c1;      // TMA coordinates of the box (y, x)
+    int ncw;         // consumer warps
 };
 
 __device__ __forceinline__ void pipe_issue(const Pipe &P, const CUtensorMap *tm, int i)
 {
     int s = i % kRing;
-    mbar_arrive_expect_tx(&P.bar[s], P.box_bytes);
-    tma_load_3d(P.ring + (size_t)s * P.slot_floats, tm, P.c0, P.c1, P.zfirst + i, &P.bar[s]);
+    mbar_arrive_expect_tx(&P.full[s], P.box_bytes);
+    tma_load_3d(P.ring + (size_t)s * P.slot_floats, tm, P.c0, P.c1, P.zfirst + i, &P.full[s]);
 }
 
 __device__ __forceinline__ bool pipe_wait(const Pipe &P, int i)
 {
-    return mbar_wait_bounded(&P.bar[i % kRing], (unsigned)((i / kRing) & 1));
+    return mbar_wait_bounded(&P.full[i % kRing], (unsigned)((i / kRing) & 1));
 }
 
-// After an aborted loop: wait (bounded) for every load still in flight so
-// that no TMA write lands in shared memory after the CTA has exited.
-__device__ void pipe_drain(const Pipe &P, int first_unwaited, int issued)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
-    for (int i = first_unwaited; i < issued; ++i) (void)pipe_wait(P, i);
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Consumer warp: release the slot of plane i.
+__device__ __forceinline__ void pipe_release(const Pipe &P, int i)
+{
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&P.empty[i % kRing]);
+}
+
+__device__ void pipe_init(const Pipe &P)
+{
+    for (int s = 0; s < kRing; ++s) {
+        mbar_init(&P.full[s], 1);
+        mbar_init(&P.empty[s], P.ncw);
+    }
+    fence_barrier_init();
+}
+
+// Refills, done by thread 0 of the CTA (which also computes).  Before
+// iteration t it issues every plane whose slot has been released, and blocks
+// only for the plane iteration t needs (t + 10) -- i.e. only when some warp
+// is more than two planes behind.  That wait needs planes <= t + 7, all
+// issued earlier, so it cannot deadlock.  Returns false on a timed-out wait.
+__device__ bool pipe_refill(const Pipe &P, const CUtensorMap *tm, int t, int &next_issue)
+{
+    while (next_issue < P.nplanes) {
+        const int i = next_issue;
+        uint64_t *e = &P.empty[i % kRing];
+        const unsigned par = (unsigned)(((i - kRing) / kRing) & 1);
+        if (i <= t + 2 * kRadius) {
+            if (!mbar_wait_bounded(e, par)) return false;
+        } else if (!mbar_try_wait(e, par)) {
+            break;
+        }
+        fence_proxy_async();
+        pipe_issue(P, tm, i);
+        ++next_issue;
+    }
+    return true;
+}
+
+// After an aborted loop (thread 0): wait, bounded, for the loads still in
+// flight so that none lands in shared memory after the CTA has exited.
+__device__ void pipe_drain(const Pipe &P, int next_issue)
+{
+    for (int j = max(0, next_issue - kRing); j < next_issue; ++j) (void)pipe_wait(P, j);
+}
+
+__device__ __forceinline__ void pipe_setup(Pipe &P, unsigned char *smem, const PlaneParams &p,
+                                           int y0, int x0, int z0, int nzc)
+{
+    const SmemLayout L = smem_layout(p.tile_x, p.pml);
+    P.ring = reinterpret_cast<float *>(smem);
+    P.full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
+    P.empty = P.full + kRing;
+    P.slot_floats = L.slot_floats;
+    P.box_bytes = (unsigned)((p.tile_x + 2 * kRadius) * kBoxY * 4);
+    P.nplanes = nzc + 2 * kRadius;
+    P.zfirst = z0 - kRadius;
+    P.c0 = y0 - kHaloY;
+    P.c1 = x0 - kRadius;
+    P.ncw = (kQuadsY * p.tile_x + 31) / 32;
 }
 
 // ---------------------------------------------------------------------------
-// gradmax kernel
+// gradmax kernel.  With QUEUE the thread keeps its own column of the last 11
+// planes in registers (loop unrolled by 11 so the queue never moves), which
+// leaves 16 shared-memory vector loads per quad and plane instead of 25.
 // ---------------------------------------------------------------------------
+template <bool QUEUE>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_gradmax_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    const SmemLayout L = smem_layout(p.tile_x, p.pml);
-    Pipe P;
-    P.ring = reinterpret_cast<float *>(smem);
-    P.bar = reinterpret_cast<uint64_t *>(smem + L.bar_off);
-    P.slot_floats = L.slot_floats;
-    P.box_bytes = (unsigned)((p.tile_x + 2 * kRadius) * kBoxY * 4);
-
     const int tid = threadIdx.x;
     const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
     const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
@@ -317,59 +379,115 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
     if (z0 >= z1) return;
     const int nzc = z1 - z0;
-    P.nplanes = nzc + 2 * kRadius;
-    P.zfirst = z0 - kRadius;
-    P.c0 = y0 - kHaloY;
-    P.c1 = x0 - kRadius;
-
+    Pipe P;
+    pipe_setup(P, smem, p, y0, x0, z0, nzc);
+    int next_issue = 0;
+    if (tid == 0) {
+        pipe_init(P);
+        next_issue = min(kRing, P.nplanes);
+        for (int i = 0; i < next_issue; ++i) pipe_issue(P, &tm_u, i);
+    }
+    __syncthreads();
     const int x = x0 + r, yq = y0 + 4 * q;
     const bool row_ok = (r < p.tile_x) && (x < p.nx - kRadius);
     bool cell_ok[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < p.ny - kRadius);
     const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
-
-    if (tid == 0) {
-        for (int s = 0; s < kRing; ++s) mbar_init(&P.bar[s], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    int issued = 0;
-    if (tid == 0) {
-        issued = min(kRing, P.nplanes);
-        for (int i = 0; i < issued; ++i) pipe_issue(P, &tm_u, i);
-    }
+    const Coefs &k = p.k;
 
     float mx = 0.0f;
     bool ok = true;
-    int waited = 0;   // planes [0, waited) are complete (thread-local view)
-    for (int t = 0; t < nzc; ++t) {
-        int need = t + 2 * kRadius;
-        while (ok && waited <= need) {
-            ok = pipe_wait(P, waited);
-            if (ok) ++waited;
-        }
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicOr(p.err, kErrWaitTimeout);
-            break;
-        }
-        if (row_ok) {
-            float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
-            quad_derivs<false>(P.ring, P.slot_floats, t, rc, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+    if (QUEUE) {
+        float4 zq[2 * kRadius + 1];
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (cell_ok[j])
-                    mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+        for (int i = 0; i < 2 * kRadius; ++i) {
+            ok = ok && pipe_wait(P, i);
+            zq[i] = lds4(P.ring + (size_t)(i % kRing) * P.slot_floats + rc);
         }
-        __syncthreads();
-        if (tid == 0 && t + kRing < P.nplanes) {
-            fence_proxy_async();
-            pipe_issue(P, &tm_u, t + kRing);
-            issued = t + kRing + 1;
+        for (int t0 = 0; t0 < nzc && ok; t0 += 2 * kRadius + 1) {
+#pragma unroll
+            for (int u = 0; u < 2 * kRadius + 1; ++u) {
+                const int t = t0 + u;
+                if (t >= nzc) break;
+                if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) {
+                    ok = false;
+                    break;
+                }
+                if (!pipe_wait(P, t + 2 * kRadius)) {
+                    ok = false;
+                    break;
+                }
+                zq[(u + 2 * kRadius) % 11] =
+                    lds4(P.ring + (size_t)((t + 2 * kRadius) % kRing) * P.slot_floats + rc);
+                const float *pc = P.ring + (size_t)((t + kRadius) % kRing) * P.slot_floats;
+                if (row_ok) {
+                    float Ux[4], Uy[4], Uz[4];
+                    float Y[20];
+#pragma unroll
+                    for (int b = 0; b < 5; ++b) {
+                        float4 v = lds4(pc + rc - 8 + 4 * b);
+                        Y[4 * b] = v.x; Y[4 * b + 1] = v.y; Y[4 * b + 2] = v.z; Y[4 * b + 3] = v.w;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float g = 0.0f;
+#pragma unroll
+                        for (int m = 0; m < kRadius; ++m) {
+                            float d = __fsub_rn(Y[8 + j + m + 1], Y[8 + j - m - 1]);
+                            g = (m == 0) ? __fmul_rn(k.cy[0], d) : fmaf(k.cy[m], d, g);
+                        }
+                        Uy[j] = g;
+                    }
+#pragma unroll
+                    for (int m = 0; m < kRadius; ++m) {
+                        float4 a = lds4(pc + rc + (m + 1) * kBoxY);
+                        float4 b = lds4(pc + rc - (m + 1) * kBoxY);
+                        float4 za = zq[(u + kRadius + m + 1) % 11];
+                        float4 zb = zq[(u + kRadius - m - 1 + 11) % 11];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            float dx_ = __fsub_rn(f4(a, j), f4(b, j));
+                            float dz_ = __fsub_rn(f4(za, j), f4(zb, j));
+                            Ux[j] = (m == 0) ? __fmul_rn(k.cx[0], dx_) : fmaf(k.cx[m], dx_, Ux[j]);
+                            Uz[j] = (m == 0) ? __fmul_rn(k.cz[0], dz_) : fmaf(k.cz[m], dz_, Uz[j]);
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (cell_ok[j])
+                            mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+                }
+                pipe_release(P, t);
+            }
+        }
+    } else {
+        int waited = 0;
+        for (int t = 0; t < nzc; ++t) {
+            if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) {
+                ok = false;
+                break;
+            }
+            while (ok && waited <= t + 2 * kRadius) {
+                ok = pipe_wait(P, waited);
+                if (ok) ++waited;
+            }
+            if (!ok) break;
+            if (row_ok) {
+                float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+                quad_derivs<false>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (cell_ok[j])
+                        mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+            }
+            pipe_release(P, t);
         }
     }
-    if (!ok && tid == 0) pipe_drain(P, waited, issued);
-    // warp reduce, one atomic per warp
+    if (!ok) {
+        atomicOr(p.err, kErrWaitTimeout);
+        if (tid == 0) pipe_drain(P, next_issue);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((tid & 31) == 0 && mx > 0.0f) atomicMax(p.gmax_bits, __float_as_uint(mx));
@@ -402,19 +520,27 @@ __device__ __forceinline__ float pml_cell(int f, float4 lc, float KS, float e2, 
     return __fadd_rn(__fadd_rn(nw13, nw21), nw33);
 }
 
+__device__ __forceinline__ float4 ldg4(const float *p)
+{
+    return __ldg(reinterpret_cast<const float4 *>(p));
+}
+
+__device__ __forceinline__ float4 ld4(const float *p)
+{
+    return *reinterpret_cast<const float4 *>(p);
+}
+
 // ---------------------------------------------------------------------------
-// step kernel
+// step kernel.  PREFETCH: the next plane's u(k-1), K, E2, R8 are loaded into
+// registers one iteration ahead; the PML state of a PML quad is loaded before
+// the stencil.  Both variants compute the same arithmetic.
 // ---------------------------------------------------------------------------
+template <bool PREFETCH>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const SmemLayout L = smem_layout(p.tile_x, p.pml);
-    Pipe P;
-    P.ring = reinterpret_cast<float *>(smem);
-    P.bar = reinterpret_cast<uint64_t *>(smem + L.bar_off);
-    P.slot_floats = L.slot_floats;
-    P.box_bytes = (unsigned)((p.tile_x + 2 * kRadius) * kBoxY * 4);
     float4 *tab = reinterpret_cast<float4 *>(smem + L.tab_off);
     SrcEntry *csrc = reinterpret_cast<SrcEntry *>(smem + L.src_off);
     float *misc = reinterpret_cast<float *>(smem + L.misc_off);
@@ -427,26 +553,15 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
     if (z0 >= z1) return;
     const int nzc = z1 - z0;
-    P.nplanes = nzc + 2 * kRadius;
-    P.zfirst = z0 - kRadius;
-    P.c0 = y0 - kHaloY;
-    P.c1 = x0 - kRadius;
+    Pipe P;
+    pipe_setup(P, smem, p, y0, x0, z0, nzc);
 
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml;
-    const int x = x0 + r, yq = y0 + 4 * q;
-    const bool row_ok = (r < p.tile_x) && (x < nx - kRadius);
-    bool cell_ok[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < ny - kRadius);
-    const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
-    // A quad is "interior in x,y" when all four cells are outside the x and
-    // y faces; then only the z faces can make it a PML quad.
-    const bool xy_interior = (x >= pml) && (x < nx - pml) && (yq >= pml) && (yq + 3 < ny - pml);
-    const int hy = ny - 2 * pml;
-
+    int next_issue = 0;
     if (tid == 0) {
-        for (int s = 0; s < kRing; ++s) mbar_init(&P.bar[s], 1);
-        fence_barrier_init();
+        pipe_init(P);
+        next_issue = min(kRing, P.nplanes);
+        for (int i = 0; i < next_issue; ++i) pipe_issue(P, &tm_u, i);
         misc[0] = threshold_m2(*p.gmax);
         int n = 0;
         for (int e = 0; e < p.nsrc; ++e) {
@@ -461,36 +576,60 @@ __global__ void __launch_bounds__(kThreads, 2)
     __syncthreads();
     const float T2 = misc[0];
     const int ncsrc = misc_i[0];
-    int issued = 0;
-    if (tid == 0) {
-        issued = min(kRing, P.nplanes);
-        for (int i = 0; i < issued; ++i) pipe_issue(P, &tm_u, i);
-    }
 
+    const int x = x0 + r, yq = y0 + 4 * q;
+    const bool row_ok = (r < p.tile_x) && (x < nx - kRadius);
+    bool cell_ok[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < ny - kRadius);
+    const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
+    const bool xy_interior = (x >= pml) && (x < nx - pml) && (yq >= pml) && (yq + 3 < ny - pml);
+    const int hy = ny - 2 * pml;
     const Coefs &k = p.k;
     const float dt = p.dt;
+
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    long long base = (long long)z0 * p.plane + (long long)x * p.ldy + yq;
+    float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
+    if (PREFETCH && row_ok) {
+        u1v = ld4(p.u_io + base);
+        Kv = ldg4(p.prm_k + base);
+        Ev = ldg4(p.prm_e + base);
+        Rv = ldg4(p.prm_r + base);
+    }
     bool ok = true;
     int waited = 0;
-    for (int t = 0; t < nzc; ++t) {
+    for (int t = 0; t < nzc; ++t, base += p.plane) {
         const int z = z0 + t;
-        const long long base = (long long)z * p.plane + (long long)x * p.ldy + yq;
-        // Global loads of this plane's per-cell data, issued before the wait.
-        float4 u1v = make_float4(0.f, 0.f, 0.f, 0.f), Kv = u1v, Ev = u1v, Rv = u1v;
-        if (row_ok) {
-            u1v = *reinterpret_cast<const float4 *>(p.u_io + base);
-            Kv = __ldg(reinterpret_cast<const float4 *>(p.prm_k + base));
-            Ev = __ldg(reinterpret_cast<const float4 *>(p.prm_e + base));
-            Rv = __ldg(reinterpret_cast<const float4 *>(p.prm_r + base));
+        float4 nu1 = zero4, nK = zero4, nE = zero4, nR = zero4;
+        if (PREFETCH) {
+            if (row_ok && t + 1 < nzc) {
+                nu1 = ld4(p.u_io + base + p.plane);
+                nK = ldg4(p.prm_k + base + p.plane);
+                nE = ldg4(p.prm_e + base + p.plane);
+                nR = ldg4(p.prm_r + base + p.plane);
+            }
+        } else if (row_ok) {
+            u1v = ld4(p.u_io + base);
+            Kv = ldg4(p.prm_k + base);
+            Ev = ldg4(p.prm_e + base);
+            Rv = ldg4(p.prm_r + base);
         }
-        const int need = t + 2 * kRadius;
-        while (ok && waited <= need) {
+        const bool pml_quad = row_ok && !(xy_interior && z >= pml && z < nz - pml);
+        float4 w11 = zero4, w12 = zero4, w31 = zero4, w32 = zero4, p1 = zero4, p2 = zero4,
+               w21 = zero4;
+        if (PREFETCH && pml_quad) {
+            w11 = ld4(p.w1o + base); w12 = ld4(p.w1c + base);
+            w31 = ld4(p.w3o + base); w32 = ld4(p.w3c + base);
+            p1 = ld4(p.po + base);   p2 = ld4(p.pc + base);
+            w21 = ld4(p.w21 + base);
+        }
+        if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) ok = false;
+        while (ok && waited <= t + 2 * kRadius) {
             ok = pipe_wait(P, waited);
             if (ok) ++waited;
         }
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicOr(p.err, kErrWaitTimeout);
-            break;
-        }
+        if (!ok) break;
         if (row_ok) {
             float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
             quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
@@ -515,21 +654,19 @@ __global__ void __launch_bounds__(kThreads, 2)
                 KS[j] = __fmul_rn(f4(Kv, j), s);
             }
             float out[4];
-            const bool interior = xy_interior && z >= pml && z < nz - pml;
-            if (interior) {
+            if (!pml_quad) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
                     out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
                 }
             } else {
-                const float4 w11 = *reinterpret_cast<const float4 *>(p.w1o + base);
-                const float4 w12 = *reinterpret_cast<const float4 *>(p.w1c + base);
-                const float4 w31 = *reinterpret_cast<const float4 *>(p.w3o + base);
-                const float4 w32 = *reinterpret_cast<const float4 *>(p.w3c + base);
-                const float4 p1 = *reinterpret_cast<const float4 *>(p.po + base);
-                const float4 p2 = *reinterpret_cast<const float4 *>(p.pc + base);
-                const float4 w21 = *reinterpret_cast<const float4 *>(p.w21 + base);
+                if (!PREFETCH) {
+                    w11 = ld4(p.w1o + base); w12 = ld4(p.w1c + base);
+                    w31 = ld4(p.w3o + base); w32 = ld4(p.w3c + base);
+                    p1 = ld4(p.po + base);   p2 = ld4(p.pc + base);
+                    w21 = ld4(p.w21 + base);
+                }
                 float n13[4], n21[4], n33[4], n3[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -586,14 +723,15 @@ __global__ void __launch_bounds__(kThreads, 2)
                 }
             }
         }
-        __syncthreads();
-        if (tid == 0 && t + kRing < P.nplanes) {
-            fence_proxy_async();
-            pipe_issue(P, &tm_u, t + kRing);
-            issued = t + kRing + 1;
+        pipe_release(P, t);
+        if (PREFETCH) {
+            u1v = nu1; Kv = nK; Ev = nE; Rv = nR;
         }
     }
-    if (!ok && tid == 0) pipe_drain(P, waited, issued);
+    if (!ok) {
+        atomicOr(p.err, kErrWaitTimeout);
+        if (tid == 0) pipe_drain(P, next_issue);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -672,24 +810,40 @@ __global__ void qp3d_params_kernel(float *K, float *E2, float *R8, long long n, 
 // ---------------------------------------------------------------------------
 cudaError_t configure_kernels()
 {
-    cudaError_t e = cudaFuncSetAttribute(qp3d_step_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(qp3d_gradmax_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                200 * 1024);
+    const int bytes = 200 * 1024;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(qp3d_step_kernel<true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(qp3d_step_kernel<false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(qp3d_gradmax_kernel<true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    return cudaFuncSetAttribute(qp3d_gradmax_kernel<false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
+static inline int plane_threads(int tile_x) { return kQuadsY * tile_x; }
+
 cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
-                           cudaStream_t stream)
+                           cudaStream_t stream, int variant)
 {
-    qp3d_gradmax_kernel<<<grid, kQuadsY * p.tile_x, smem, stream>>>(tm_u, p);
+    if (variant == 0)
+        qp3d_gradmax_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+    else
+        qp3d_gradmax_kernel<true><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
-                        cudaStream_t stream)
+                        cudaStream_t stream, int variant)
 {
-    qp3d_step_kernel<<<grid, kQuadsY * p.tile_x, smem, stream>>>(tm_u, p);
+    if (variant == 0)
+        qp3d_step_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+    else
+        qp3d_step_kernel<true><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
     return cudaGetLastError();
 }
 

@@ -50,7 +50,8 @@ EXPORTS = [
     "qp3d_shot_advance", "qp3d_shot_sync", "qp3d_shot_step", "qp3d_shot_read_record",
     "qp3d_shot_read_uxyzmax", "qp3d_shot_snapshot", "qp3d_pml_state_size",
     "qp3d_shot_write_state", "qp3d_shot_read_state", "qp3d_shot_time",
-    "qp3d_shot_launches_per_step", "qp3d_event_record", "qp3d_event_elapsed",
+    "qp3d_shot_launches_per_step", "qp3d_tune", "qp3d_tune_get", "qp3d_event_record",
+    "qp3d_event_elapsed",
     "qp3d_host_alloc", "qp3d_host_free", "qp3d_fdcoff1", "qp3d_fdcoff2", "qp3d_pmlcoff",
     "qp3d_source", "qp3d_extend_model", "qp3d_absmax", "qp3d_readmodel3d",
 ]
@@ -88,6 +89,8 @@ def load():
         "qp3d_shot_time": (ctypes.c_int, [_vp, ctypes.c_int, P(ctypes.c_float),
                                           P(ctypes.c_float), P(ctypes.c_float)]),
         "qp3d_shot_launches_per_step": (ctypes.c_int, [_vp]),
+        "qp3d_tune": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
+        "qp3d_tune_get": (ctypes.c_int, [_vp, ctypes.c_char_p]),
         "qp3d_event_record": (ctypes.c_int, [_vp, ctypes.c_int]),
         "qp3d_event_elapsed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int,
                                               P(ctypes.c_float)]),
@@ -338,6 +341,13 @@ class Context:
 
     def launches_per_step(self):
         return int(self._L.qp3d_shot_launches_per_step(self.h))
+
+    def tune(self, **kv):
+        for key, value in kv.items():
+            self._check(self._L.qp3d_tune(self.h, key.encode(), int(value)), "qp3d_tune " + key)
+
+    def tuning(self, key):
+        return int(self._L.qp3d_tune_get(self.h, key.encode()))
 
     def event(self, slot):
         self._check(self._L.qp3d_event_record(self.h, slot), "qp3d_event_record")

@@ -125,6 +125,15 @@ int qp3d_shot_time(qp3d_ctx *ctx, int nsteps, float *ms_total, float *ms_step,
 /* Number of kernels the library launches per time step for the loaded shot. */
 int qp3d_shot_launches_per_step(const qp3d_ctx *ctx);
 
+/* Launch tuning (autotuner hook).  Keys: "step_variant" (0: loads at use,
+ * 1: next-plane prefetch), "gradmax_variant" (0: shared-memory z taps,
+ * 1: register queue), "tile_x" (rows per tile, 0 = automatic),
+ * "chunks" (z chunks, 0 = automatic).  Takes effect at the next
+ * qp3d_shot_load, or immediately for the loaded shot.  All settings compute
+ * identical results. */
+int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
+int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
+
 /* CUDA events on the context's stream, for timing any sequence of library
  * calls on the stream the kernels run on.  slot in [0, 8). */
 int qp3d_event_record(qp3d_ctx *ctx, int slot);

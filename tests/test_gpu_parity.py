@@ -243,3 +243,23 @@ def test_timing_helper(ctx):
     total, ms_step, ms_grad = ctx.time(10)
     assert total > 0 and ms_step > 0 and ms_grad > 0
     assert ms_step + ms_grad <= total * 1.05 + 0.05
+
+
+@pytest.mark.parametrize("step_v,grad_v,tile_x,chunks", [(0, 0, 0, 0), (1, 1, 0, 0),
+                                                         (1, 0, 17, 3), (0, 1, 32, 1),
+                                                         (1, 1, 9, 5)])
+def test_tuning_settings_are_bit_identical(ctx, step_v, grad_v, tile_x, chunks):
+    """Every launch variant, tile height and z-chunking computes the same bits
+    as the oracle mirror (the autotuner may pick any of them)."""
+    shot = synthetic.small_case(hx=30, hy=34, nz0=40, pml=8, nt=30, seed=12)
+    ctx.tune(step_variant=step_v, gradmax_variant=grad_v, tile_x=tile_x, chunks=chunks)
+    try:
+        rec = ctx.forward(shot)
+        ctx.load(shot)
+        ctx.advance(shot.nt)
+        mx = ctx.uxyzmax()
+    finally:
+        ctx.tune(step_variant=1, gradmax_variant=1, tile_x=0, chunks=0)
+    mrec, mmx, _ = O.run(O.MIRROR, shot.to_oracle(O))
+    assert bits_equal(rec, mrec)
+    assert bits_equal(mx, mmx)
