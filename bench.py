@@ -279,6 +279,7 @@ def run_gpu_arm(args, dist):
     gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dev]
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dev)
     clocks = Clocks(gpu_index)
+    launches0 = ctx.launch_count()
     ctx.event(0)
     ms_step, ms_grad = 0.0, 0.0
     for _ in range(args.steps):
@@ -292,8 +293,8 @@ def run_gpu_arm(args, dist):
     dist.barrier()
     ms = dist.max(ms)
     value = dist.world * cells * nt * args.steps / (ms / 1e3) / 1e9
-    launches_per_step = ctx.launches_per_step()
-    gpu_launches = (launches_per_step * nt + 2 * snaps_per_shot) * args.steps
+    gpu_launches = ctx.launch_count() - launches0
+    redo, alt = ctx.stats(0, nt)
 
     # roofline of the fused step kernel (one launch = one time step)
     bstep, ni, np_ = algorithmic_bytes(shot)
@@ -311,8 +312,11 @@ def run_gpu_arm(args, dist):
                 "traffic_note": ("ncu dram read+write of one launch on %s, scaled per cell" % tcase)
                 if tpc else "no ncu capture committed",
                 "step_kernel_ms": round(ms_step / n_launch, 5),
-                "gradmax_kernel_ms": round(ms_grad / n_launch, 5),
-                "gradmax_read_bytes": 4 * cells}
+                "threshold_overhead_ms": round(ms_grad / n_launch, 5),
+                "threshold_note": "per step: gradmax pre-pass for the first 3 steps, then the "
+                                  "fix-up kernel and the gated exact re-run of the speculative "
+                                  "step; last shot: %d re-runs in %d steps, max %d deferred "
+                                  "cells per step" % (int(redo.sum()), nt, int(alt.max()))}
 
     # end to end through the C ABI from pinned host memory
     pin = {}

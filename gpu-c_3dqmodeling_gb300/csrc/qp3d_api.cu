@@ -46,21 +46,29 @@ struct qp3d_ctx {
     int tile_x = 0, nxt = 0, nyt = 0, nchunks = 0, chunk_z = 0;
     size_t smem = 0;
     bool rec_fused = true;
-    float *U[2] = {nullptr, nullptr};
+    float *U[3] = {nullptr, nullptr, nullptr};
     float *K = nullptr, *E2 = nullptr, *R8 = nullptr;
-    float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21 = nullptr;
+    float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21[2] = {};
     float *record = nullptr;
     float *gmax = nullptr;
+    // speculative threshold: per-step window, re-run flags, alternatives
+    float *win = nullptr;
+    int *redo = nullptr;
+    unsigned *alt_count = nullptr;
+    float *spec_err = nullptr;
+    AltEntry *alt = nullptr;
+    unsigned alt_cap = 0;
     float4 *layers = nullptr;
     SrcEntry *src_fused = nullptr, *src_band = nullptr, *src_all = nullptr;
     int n_fused = 0, n_band = 0, n_all = 0;
     bool fuse_sources = true;
     unsigned *errword = nullptr;
-    CUtensorMap tm[2];
+    CUtensorMap tm[3];
     Coefs coefs{};
     std::vector<float> wavelet;
     int step = 0;
     int cur = 0;           // U[cur] holds u(step)
+    int prev = 1;          // U[prev] holds u(step-1); the third buffer receives u(step+1)
     // snapshot staging
     float *snap_dev = nullptr;
     float *snap_host = nullptr;
@@ -68,7 +76,11 @@ struct qp3d_ctx {
     cudaEvent_t ev[4] = {};
     cudaEvent_t uev[8] = {};
     // tuning
-    int step_variant = 1, gradmax_variant = 1, tune_tile_x = 0, tune_chunks = 0;
+    int step_variant = 0, gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
+    int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
+    float delta_min = 0.005f;        // smallest half-width of the predicted window
+    unsigned tune_alt_cap = 0;
+    long long launches = 0;          // kernels launched by this context
 };
 
 // ---------------------------------------------------------------------------
@@ -89,6 +101,13 @@ static int fail(qp3d_ctx *c, int code, const char *fmt, ...)
         if (e_ != cudaSuccess)                                                             \
             return fail(ctx, e_ == cudaErrorMemoryAllocation ? QP3D_ERR_NOMEM : QP3D_ERR_CUDA, \
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// launch a library kernel: check it and count it
+#define CKL(call)                                                                          \
+    do {                                                                                   \
+        CK(call);                                                                          \
+        ++ctx->launches;                                                                   \
     } while (0)
 
 extern "C" int qp3d_version(void) { return 10000; }
@@ -113,14 +132,22 @@ extern "C" const char *qp3d_ctx_last_error(const qp3d_ctx *ctx) { return ctx ? c
 static void free_shot(qp3d_ctx *ctx)
 {
     cudaSetDevice(ctx->device);
-    float **bufs[] = {&ctx->U[0], &ctx->U[1], &ctx->K,     &ctx->E2,    &ctx->R8,
-                      &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0], &ctx->W3[1],
-                      &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],  &ctx->W21,
-                      &ctx->record, &ctx->gmax, &ctx->snap_dev};
+    float **bufs[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->K,     &ctx->E2,
+                      &ctx->R8,    &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0],
+                      &ctx->W3[1], &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],
+                      &ctx->W21[0], &ctx->W21[1], &ctx->record, &ctx->gmax, &ctx->snap_dev,
+                      &ctx->win,   &ctx->spec_err};
     for (float **b : bufs) {
         if (*b) cudaFree(*b);
         *b = nullptr;
     }
+    if (ctx->redo) cudaFree(ctx->redo);
+    if (ctx->alt_count) cudaFree(ctx->alt_count);
+    if (ctx->alt) cudaFree(ctx->alt);
+    ctx->redo = nullptr;
+    ctx->alt_count = nullptr;
+    ctx->alt = nullptr;
+    ctx->alt_cap = 0;
     if (ctx->layers) cudaFree(ctx->layers);
     if (ctx->src_fused) cudaFree(ctx->src_fused);
     if (ctx->src_band) cudaFree(ctx->src_band);
@@ -285,9 +312,10 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     plan_launch(ctx);
 
     if (!same) {
-        float **vols[] = {&ctx->U[0], &ctx->U[1], &ctx->K,     &ctx->E2,    &ctx->R8,
-                          &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0], &ctx->W3[1],
-                          &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],  &ctx->W21};
+        float **vols[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->K,     &ctx->E2,
+                          &ctx->R8,    &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0],
+                          &ctx->W3[1], &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],
+                          &ctx->W21[0], &ctx->W21[1]};
         for (float **v : vols)
             if ((rc = alloc_vol(ctx, v))) {
                 free_shot(ctx);
@@ -298,12 +326,21 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         CK(cudaMalloc(&ctx->gmax, (size_t)std::max(g->nt, 1) * sizeof(float)));
         CK(cudaMalloc(&ctx->layers, sizeof(float4) * 3 * std::max(g->pml, 1)));
         if (!ctx->errword) CK(cudaMalloc(&ctx->errword, sizeof(unsigned)));
+        size_t ntb = (size_t)std::max(g->nt, 1);
+        CK(cudaMalloc(&ctx->win, 3 * ntb * sizeof(float)));
+        CK(cudaMalloc(&ctx->redo, ntb * sizeof(int)));
+        CK(cudaMalloc(&ctx->alt_count, ntb * sizeof(unsigned)));
+        CK(cudaMalloc(&ctx->spec_err, sizeof(float)));
+        long long cap = ctx->tune_alt_cap ? (long long)ctx->tune_alt_cap
+                                          : std::max(1ll << 20, ctx->vol / 16);
+        ctx->alt_cap = (unsigned)std::min(cap, (long long)0x7fffffff);
+        CK(cudaMalloc(&ctx->alt, (size_t)ctx->alt_cap * sizeof(AltEntry)));
     }
     // model -> per-cell parameters (K, E2, R8 hold vp, eps, delta first)
     if ((rc = upload_vol(ctx, ctx->K, m->vp)) || (rc = upload_vol(ctx, ctx->E2, m->epsilon)) ||
         (rc = upload_vol(ctx, ctx->R8, m->delta)))
         return rc;
-    CK(launch_params(nullptr, nullptr, nullptr, ctx->K, ctx->E2, ctx->R8, ctx->vol, g->dt,
+    CKL(launch_params(nullptr, nullptr, nullptr, ctx->K, ctx->E2, ctx->R8, ctx->vol, g->dt,
                      ctx->stream));
     // coefficient tables
     derive_coefs(m->c, m->c2, g->dx, g->dy, g->dz, &ctx->coefs);
@@ -355,8 +392,8 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     // lies inside the updated box
     ctx->rec_fused = g->pml >= kRadius && g->sz >= kRadius && g->sz < g->nz - kRadius &&
                      ctx->fuse_sources && ctx->n_band == 0;
-    if ((rc = make_tmap(ctx, ctx->U[0], &ctx->tm[0])) || (rc = make_tmap(ctx, ctx->U[1], &ctx->tm[1])))
-        return rc;
+    for (int i = 0; i < 3; ++i)
+        if ((rc = make_tmap(ctx, ctx->U[i], &ctx->tm[i]))) return rc;
     ctx->loaded = true;
     return qp3d_shot_reset(ctx);
 }
@@ -367,9 +404,16 @@ extern "C" int qp3d_shot_reset(qp3d_ctx *ctx)
     if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
     CK(cudaSetDevice(ctx->device));
     size_t vb = (size_t)ctx->vol * sizeof(float);
-    float *zero[] = {ctx->U[0], ctx->U[1], ctx->W1[0], ctx->W1[1], ctx->W1[2], ctx->W3[0],
-                     ctx->W3[1], ctx->W3[2], ctx->P[0],  ctx->P[1],  ctx->P[2],  ctx->W21};
+    float *zero[] = {ctx->U[0],  ctx->U[1],  ctx->U[2],  ctx->W1[0], ctx->W1[1], ctx->W1[2],
+                     ctx->W3[0], ctx->W3[1], ctx->W3[2], ctx->P[0],  ctx->P[1],  ctx->P[2],
+                     ctx->W21[0], ctx->W21[1]};
     for (float *p : zero) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
+    size_t ntb = (size_t)std::max(ctx->g.nt, 1);
+    CK(cudaMemsetAsync(ctx->win, 0, 3 * ntb * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(ctx->redo, 0, ntb * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->alt_count, 0, ntb * sizeof(unsigned), ctx->stream));
+    static const float one = 1.0f;
+    CK(cudaMemcpyAsync(ctx->spec_err, &one, sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(ctx->gmax, 0, sizeof(float) * std::max(ctx->g.nt, 1), ctx->stream));
     CK(cudaMemsetAsync(ctx->record, 0,
                        sizeof(float) * (size_t)std::max(ctx->g.nt, 1) * ctx->hx * ctx->hy,
@@ -377,16 +421,28 @@ extern "C" int qp3d_shot_reset(qp3d_ctx *ctx)
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(unsigned), ctx->stream));
     ctx->step = 0;
     ctx->cur = 0;
+    ctx->prev = 1;
     return QP3D_OK;
 }
 
-// Enqueue one time step.  ev_* are optional events bracketing the kernels.
+// Speculative threshold handling is used from this step on (the window is
+// predicted from the two previous maxima).
+constexpr int kSpecFirstStep = 3;
+
+static bool use_spec(const qp3d_ctx *ctx, int k)
+{
+    return ctx->threshold_mode == 1 && k >= kSpecFirstStep && ctx->vol < (1ll << 32);
+}
+
+// Enqueue one time step.  ev_* are optional events bracketing the main step
+// kernel (s) and the threshold overhead kernels (g: gradmax, or fix-up plus
+// the gated exact re-run).
 static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cudaEvent_t ev_s0,
                         cudaEvent_t ev_s1)
 {
     const qp3d_geom &g = ctx->g;
     const int k = ctx->step;
-    const int a = ctx->cur, b = a ^ 1;
+    const int a = ctx->cur, b = ctx->prev, c = 3 - a - b;
     PlaneParams p;
     memset(&p, 0, sizeof(p));
     p.nx = g.nx; p.ny = g.ny; p.nz = g.nz; p.ldy = ctx->ldy; p.pml = g.pml; p.sz = g.sz;
@@ -397,40 +453,63 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.dt = g.dt;
     p.step = k;
     p.wavelet = ctx->wavelet[k];
-    p.u_io = ctx->U[b];
+    p.u_prev = ctx->U[b];
+    p.u_out = ctx->U[c];
     p.prm_k = ctx->K; p.prm_e = ctx->E2; p.prm_r = ctx->R8;
     const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
     p.w1o = ctx->W1[lo]; p.w1c = ctx->W1[lc]; p.w1n = ctx->W1[ln];
     p.w3o = ctx->W3[lo]; p.w3c = ctx->W3[lc]; p.w3n = ctx->W3[ln];
     p.po = ctx->P[lo];   p.pc = ctx->P[lc];   p.pn = ctx->P[ln];
-    p.w21 = ctx->W21;
+    p.w21o = ctx->W21[k % 2];
+    p.w21n = ctx->W21[(k + 1) % 2];
     p.layers = ctx->layers;
-    p.gmax = ctx->gmax + k;
-    p.gmax_bits = reinterpret_cast<unsigned *>(ctx->gmax + k);
+    p.gmax = ctx->gmax;
     float *rec_plane = ctx->record + (size_t)k * ctx->hx * ctx->hy;
     p.record = ctx->rec_fused ? rec_plane : nullptr;
     p.src = ctx->fuse_sources ? ctx->src_fused : nullptr;
     p.nsrc = ctx->fuse_sources ? ctx->n_fused : 0;
     p.err = ctx->errword;
+    p.delta_min = ctx->delta_min;
     dim3 grid(ctx->nyt, ctx->nxt, ctx->nchunks);
 
-    if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
-    CK(launch_gradmax(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->gradmax_variant));
-    if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
-    if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
-    CK(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->step_variant));
-    if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
-    if (ctx->fuse_sources) {
-        CK(launch_band_sources(ctx->U[b], ctx->U[a], ctx->src_band, ctx->n_band, ctx->plane,
-                               ctx->ldy, p.wavelet, ctx->stream));
+    if (use_spec(ctx, k)) {
+        p.spec = 1;
+        p.win = ctx->win + 3 * (size_t)k;
+        p.spec_err = ctx->spec_err;
+        p.alt = ctx->alt;
+        p.alt_count = ctx->alt_count + k;
+        p.alt_cap = ctx->alt_cap;
+        if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
+        CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->step_variant));
+        if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
+        if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
+        CKL(launch_fixup(p, ctx->redo + k, ctx->spec_err, ctx->stream, ctx->nsm));
+        PlaneParams pe = p;
+        pe.spec = 0;
+        pe.gate = ctx->redo + k;
+        CKL(launch_step(ctx->tm[a], pe, grid, ctx->smem, ctx->stream, ctx->step_variant));
+        if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
     } else {
-        CK(launch_all_sources(ctx->U[b], ctx->U[a], ctx->src_all, ctx->n_all, ctx->plane, ctx->ldy,
+        if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
+        CKL(launch_gradmax(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->gradmax_variant));
+        if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
+        if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
+        CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->step_variant));
+        if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
+    }
+    if (ctx->fuse_sources) {
+        if (ctx->n_band > 0)
+            CKL(launch_band_sources(ctx->U[c], ctx->U[a], ctx->src_band, ctx->n_band, ctx->plane,
+                               ctx->ldy, p.wavelet, ctx->stream));
+    } else if (ctx->n_all > 0) {
+        CKL(launch_all_sources(ctx->U[c], ctx->U[a], ctx->src_all, ctx->n_all, ctx->plane, ctx->ldy,
                               g.nx, g.ny, g.nz, p.wavelet, ctx->stream));
     }
     if (!ctx->rec_fused)
-        CK(launch_record(ctx->U[b], rec_plane, g.nx, g.ny, g.pml, g.sz, ctx->ldy, ctx->plane,
+        CKL(launch_record(ctx->U[c], rec_plane, g.nx, g.ny, g.pml, g.sz, ctx->ldy, ctx->plane,
                          ctx->stream));
-    ctx->cur = b;
+    ctx->prev = a;
+    ctx->cur = c;
     ctx->step = k + 1;
     return QP3D_OK;
 }
@@ -438,7 +517,7 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
 extern "C" int qp3d_shot_launches_per_step(const qp3d_ctx *ctx)
 {
     if (!ctx || !ctx->loaded) return 0;
-    int n = 2;
+    int n = use_spec(ctx, ctx->step) ? 3 : 2;
     if (ctx->fuse_sources) n += ctx->n_band > 0 ? 1 : 0;
     else n += ctx->n_all > 0 ? 1 : 0;
     if (!ctx->rec_fused) n += 1;
@@ -557,7 +636,7 @@ extern "C" size_t qp3d_pml_state_size(int nx, int ny, int nz, int pml)
 static void level_arrays(qp3d_ctx *ctx, int k, float *arr[10])
 {
     const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
-    arr[0] = ctx->W1[lo]; arr[1] = ctx->W1[lc]; arr[2] = ctx->W1[ln]; arr[3] = ctx->W21;
+    arr[0] = ctx->W1[lo]; arr[1] = ctx->W1[lc]; arr[2] = ctx->W1[ln]; arr[3] = ctx->W21[k % 2];
     arr[4] = ctx->W3[lo]; arr[5] = ctx->W3[lc]; arr[6] = ctx->W3[ln];
     arr[7] = ctx->P[lo];  arr[8] = ctx->P[lc];  arr[9] = ctx->P[ln];
 }
@@ -572,7 +651,7 @@ extern "C" int qp3d_shot_write_state(qp3d_ctx *ctx, int step, const float *u_pre
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->step = step;
     int rc;
-    if (u_prev && (rc = upload_vol(ctx, ctx->U[ctx->cur ^ 1], u_prev))) return rc;
+    if (u_prev && (rc = upload_vol(ctx, ctx->U[ctx->prev], u_prev))) return rc;
     if (u_cur && (rc = upload_vol(ctx, ctx->U[ctx->cur], u_cur))) return rc;
     if (pml_state) {
         const qp3d_geom &g = ctx->g;
@@ -604,7 +683,7 @@ extern "C" int qp3d_shot_read_state(qp3d_ctx *ctx, float *u_prev, float *u_cur, 
     if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
     int rc = qp3d_shot_sync(ctx);
     if (rc) return rc;
-    if (u_prev && (rc = download_vol(ctx, u_prev, ctx->U[ctx->cur ^ 1]))) return rc;
+    if (u_prev && (rc = download_vol(ctx, u_prev, ctx->U[ctx->prev]))) return rc;
     if (u_cur && (rc = download_vol(ctx, u_cur, ctx->U[ctx->cur]))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
     if (pml_state) {
@@ -674,7 +753,7 @@ extern "C" int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap)
         size_t n = (size_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
         int rc = ensure_snap(ctx, n);
         if (rc) return rc;
-        CK(launch_crop(u, ctx->snap_dev, r.x0, r.x1, r.y0, r.y1, r.z0, r.z1, ctx->ldy, ctx->plane,
+        CKL(launch_crop(u, ctx->snap_dev, r.x0, r.x1, r.y0, r.y1, r.z0, r.z1, ctx->ldy, ctx->plane,
                        ctx->stream));
         CK(cudaMemcpyAsync(ctx->snap_host, ctx->snap_dev, n * sizeof(float), cudaMemcpyDeviceToHost,
                            ctx->stream));
@@ -789,14 +868,29 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "gradmax_variant") && (value == 0 || value == 1)) ctx->gradmax_variant = value;
     else if (!strcmp(key, "tile_x") && value >= 0 && value <= kMaxTileX) ctx->tune_tile_x = value;
     else if (!strcmp(key, "chunks") && value >= 0) ctx->tune_chunks = value;
+    else if (!strcmp(key, "threshold_mode") && (value == 0 || value == 1)) ctx->threshold_mode = value;
+    else if (!strcmp(key, "spec_delta_ppm") && value >= 0 && value <= 250000)
+        ctx->delta_min = value * 1e-6f;
+    else if (!strcmp(key, "alt_cap") && value >= 0) {
+        ctx->tune_alt_cap = (unsigned)value;
+        if (ctx->loaded) {
+            CK(cudaSetDevice(ctx->device));
+            CK(cudaStreamSynchronize(ctx->stream));
+            if (ctx->alt) cudaFree(ctx->alt);
+            ctx->alt = nullptr;
+            long long cap = value ? (long long)value : std::max(1ll << 20, ctx->vol / 16);
+            ctx->alt_cap = (unsigned)std::min(cap, (long long)0x7fffffff);
+            CK(cudaMalloc(&ctx->alt, (size_t)std::max(ctx->alt_cap, 1u) * sizeof(AltEntry)));
+        }
+    }
     else return fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
     if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
         CK(cudaSetDevice(ctx->device));
         CK(cudaStreamSynchronize(ctx->stream));
         plan_launch(ctx);
         int rc;
-        if ((rc = make_tmap(ctx, ctx->U[0], &ctx->tm[0])) || (rc = make_tmap(ctx, ctx->U[1], &ctx->tm[1])))
-            return rc;
+        for (int i = 0; i < 3; ++i)
+            if ((rc = make_tmap(ctx, ctx->U[i], &ctx->tm[i]))) return rc;
     }
     return QP3D_OK;
 }
@@ -808,5 +902,23 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "gradmax_variant")) return ctx->gradmax_variant;
     if (!strcmp(key, "tile_x")) return ctx->loaded ? ctx->tile_x : ctx->tune_tile_x;
     if (!strcmp(key, "chunks")) return ctx->loaded ? ctx->nchunks : ctx->tune_chunks;
+    if (!strcmp(key, "threshold_mode")) return ctx->threshold_mode;
+    if (!strcmp(key, "spec_delta_ppm")) return (int)(ctx->delta_min * 1e6f + 0.5f);
+    if (!strcmp(key, "alt_cap")) return (int)ctx->alt_cap;
     return QP3D_ERR_ARG;
 }
+
+extern "C" int qp3d_shot_read_stats(qp3d_ctx *ctx, int k0, int nsteps, int *redo, unsigned *alt)
+{
+    if (!ctx || k0 < 0 || nsteps < 0) return QP3D_ERR_ARG;
+    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (k0 + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "range past nt");
+    int rc = qp3d_shot_sync(ctx);
+    if (rc) return rc;
+    if (redo) CK(cudaMemcpy(redo, ctx->redo + k0, nsteps * sizeof(int), cudaMemcpyDeviceToHost));
+    if (alt)
+        CK(cudaMemcpy(alt, ctx->alt_count + k0, nsteps * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    return QP3D_OK;
+}
+
+extern "C" long long qp3d_ctx_launch_count(const qp3d_ctx *ctx) { return ctx ? ctx->launches : -1; }

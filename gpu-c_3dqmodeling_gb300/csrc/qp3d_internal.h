@@ -47,6 +47,15 @@ struct SrcEntry {
     float v;
 };
 
+// One cell whose threshold decision depended on the exact max: its u(k+1)
+// (and PML state) computed with S = 1, to be used if m2 <= T2(max).
+struct AltEntry {
+    unsigned idx;        // pitched cell index
+    float m2;            // |grad u|^2 as the kernel computed it
+    float u3, w13, p3, w21, w33;
+    unsigned pml;        // 1: the state alternatives are valid
+};
+
 struct PlaneParams {
     // geometry
     int nx, ny, nz, ldy, pml, sz;
@@ -57,20 +66,29 @@ struct PlaneParams {
     float dt;
     int step;            // time step index k
     float wavelet;       // wavelet[k]
-    // buffers
-    float *u_io;         // u(k-1) in, u(k+1) out (in place)
+    // wavefields: u(k) is staged by TMA; u(k-1) read, u(k+1) written
+    const float *u_prev;
+    float *u_out;
     const float *prm_k, *prm_e, *prm_r;
     const float *w1o, *w1c; float *w1n;   // w11, w12 -> w13
     const float *w3o, *w3c; float *w3n;   // w31, w32 -> w33
     const float *po, *pc; float *pn;      // p1, p2 -> p3
-    float *w21;
+    const float *w21o; float *w21n;       // w21 -> w21'
     const float4 *layers;     // [3][pml] (a1, a2, a3, dd) for lr, fb, tb
-    const float *gmax;        // &gmax[step]
-    unsigned *gmax_bits;      // &gmax[step] as bits (gradmax kernel)
+    float *gmax;              // gmax[0..nt): max|grad u| per step
     float *record;            // record plane of this step, or null
     const SrcEntry *src;      // sources inside the updated box, fused
     int nsrc;
     unsigned *err;
+    // threshold handling of the step kernel
+    int spec;                 // 1: predicted window, own max, alternatives list
+    const int *gate;          // exact mode: run only if *gate != 0 (null: always)
+    float *win;               // spec: &win[3*step] = (M_lo, M_hi, M_pred)
+    const float *spec_err;    // last relative prediction error of the max
+    float delta_min;          // smallest half-width of the window
+    AltEntry *alt;            // alternatives of this step
+    unsigned *alt_count;      // &alt_count[step]
+    unsigned alt_cap;
 };
 
 struct Shot;   // host-side, defined in qp3d_api.cu
@@ -81,6 +99,8 @@ cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p,
                            dim3 grid, size_t smem, cudaStream_t stream, int variant);
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p,
                         dim3 grid, size_t smem, cudaStream_t stream, int variant);
+cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
+                         int nsm);
 cudaError_t launch_band_sources(float *u_new, const float *u_cur,
                                 const SrcEntry *src, int n, long long plane,
                                 int ldy, float w, cudaStream_t stream);

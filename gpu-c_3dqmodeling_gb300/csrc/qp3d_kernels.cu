@@ -490,7 +490,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((tid & 31) == 0 && mx > 0.0f) atomicMax(p.gmax_bits, __float_as_uint(mx));
+    if ((tid & 31) == 0 && mx > 0.0f)
+        atomicMax(reinterpret_cast<unsigned *>(p.gmax + p.step), __float_as_uint(mx));
 }
 
 // ---------------------------------------------------------------------------
@@ -531,14 +532,49 @@ __device__ __forceinline__ float4 ld4(const float *p)
 }
 
 // ---------------------------------------------------------------------------
-// step kernel.  PREFETCH: the next plane's u(k-1), K, E2, R8 are loaded into
-// registers one iteration ahead; the PML state of a PML quad is loaded before
-// the stencil.  Both variants compute the same arithmetic.
+// step kernel.
+//   SPEC = false ("exact"): the threshold comes from gmax[step], already
+//     known (gradmax kernel, or a speculative pass of the same step).  With a
+//     gate the kernel runs only when *gate != 0 (the re-run of a step whose
+//     speculation failed).
+//   SPEC = true: the max of the step is not known yet.  It is predicted from
+//     the two previous steps with a window [M_lo, M_hi]; a cell whose m2 lies
+//     in (T2(M_lo), T2(M_hi)] has an uncertain decision and is computed both
+//     ways -- the S = 1 result goes to the alternatives list -- and the
+//     kernel reduces the true max of the step into gmax[step] on the way.
+//     qp3d_fixup_kernel then applies the alternatives, or asks for the exact
+//     re-run when the max fell outside the window or the list overflowed.
+//   Both modes write bit-identical results.
 // ---------------------------------------------------------------------------
-template <bool PREFETCH>
+__device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &pred)
+{
+    const int k = p.step;
+    const float m1 = k >= 1 ? p.gmax[k - 1] : 0.0f;
+    const float m0 = k >= 2 ? p.gmax[k - 2] : 0.0f;
+    float r = (m0 > 0.0f) ? __fdiv_rn(m1, m0) : 1.0f;
+    r = fminf(fmaxf(r, 0.5f), 2.0f);
+    pred = __fmul_rn(m1, r);
+    const float d = fminf(0.25f, fmaxf(p.delta_min, __fmul_rn(3.0f, *p.spec_err)));
+    lo = __fmul_rn(pred, __fsub_rn(1.0f, d));
+    hi = __fmul_rn(pred, __fadd_rn(1.0f, d));
+}
+
+// S of one cell (GPU_kernel.cu:100-111), given it is above the threshold.
+__device__ __forceinline__ float aniso_s(float h2, float m2, float e2x, float r8)
+{
+    float aa = __fdiv_rn(h2, m2);
+    float bb = __fsub_rn(1.0f, aa);
+    float den = fmaf(e2x, aa, 1.0f);
+    float num = __fmul_rn(__fmul_rn(r8, aa), bb);
+    float qq = __fdiv_rn(num, __fmul_rn(den, den));
+    return fmaf(0.5f, __fsqrt_rn(__fsub_rn(1.0f, qq)), 0.5f);
+}
+
+template <bool SPEC>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
+    if (!SPEC && p.gate && *p.gate == 0) return;
     extern __shared__ __align__(128) unsigned char smem[];
     const SmemLayout L = smem_layout(p.tile_x, p.pml);
     float4 *tab = reinterpret_cast<float4 *>(smem + L.tab_off);
@@ -546,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     float *misc = reinterpret_cast<float *>(smem + L.misc_off);
     int *misc_i = reinterpret_cast<int *>(smem + L.misc_off + 16);
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
     const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
     const int z0 = kRadius + blockIdx.z * p.chunk_z;
@@ -562,7 +598,19 @@ __global__ void __launch_bounds__(kThreads, 2)
         pipe_init(P);
         next_issue = min(kRing, P.nplanes);
         for (int i = 0; i < next_issue; ++i) pipe_issue(P, &tm_u, i);
-        misc[0] = threshold_m2(*p.gmax);
+        if (SPEC) {
+            float lo, hi, pred;
+            spec_window(p, lo, hi, pred);
+            misc[0] = threshold_m2(lo);
+            misc[1] = threshold_m2(hi);
+            if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
+                p.win[0] = lo;
+                p.win[1] = hi;
+                p.win[2] = pred;
+            }
+        } else {
+            misc[0] = misc[1] = threshold_m2(p.gmax[p.step]);
+        }
         int n = 0;
         for (int e = 0; e < p.nsrc; ++e) {
             SrcEntry s = p.src[e];
@@ -574,7 +622,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     for (int i = tid; i < 3 * pml; i += blockDim.x) tab[i] = p.layers[i];
     __syncthreads();
-    const float T2 = misc[0];
+    const float T2lo = misc[0], T2hi = misc[1];
     const int ncsrc = misc_i[0];
 
     const int x = x0 + r, yq = y0 + 4 * q;
@@ -587,49 +635,33 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int hy = ny - 2 * pml;
     const Coefs &k = p.k;
     const float dt = p.dt;
-
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    long long base = (long long)z0 * p.plane + (long long)x * p.ldy + yq;
-    float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
-    if (PREFETCH && row_ok) {
-        u1v = ld4(p.u_io + base);
-        Kv = ldg4(p.prm_k + base);
-        Ev = ldg4(p.prm_e + base);
-        Rv = ldg4(p.prm_r + base);
-    }
+
+    float mx = 0.0f;
     bool ok = true;
     int waited = 0;
+    long long base = (long long)z0 * p.plane + (long long)x * p.ldy + yq;
     for (int t = 0; t < nzc; ++t, base += p.plane) {
         const int z = z0 + t;
-        float4 nu1 = zero4, nK = zero4, nE = zero4, nR = zero4;
-        if (PREFETCH) {
-            if (row_ok && t + 1 < nzc) {
-                nu1 = ld4(p.u_io + base + p.plane);
-                nK = ldg4(p.prm_k + base + p.plane);
-                nE = ldg4(p.prm_e + base + p.plane);
-                nR = ldg4(p.prm_r + base + p.plane);
-            }
-        } else if (row_ok) {
-            u1v = ld4(p.u_io + base);
+        float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
+        if (row_ok) {
+            u1v = ldg4(p.u_prev + base);
             Kv = ldg4(p.prm_k + base);
             Ev = ldg4(p.prm_e + base);
             Rv = ldg4(p.prm_r + base);
         }
         const bool pml_quad = row_ok && !(xy_interior && z >= pml && z < nz - pml);
-        float4 w11 = zero4, w12 = zero4, w31 = zero4, w32 = zero4, p1 = zero4, p2 = zero4,
-               w21 = zero4;
-        if (PREFETCH && pml_quad) {
-            w11 = ld4(p.w1o + base); w12 = ld4(p.w1c + base);
-            w31 = ld4(p.w3o + base); w32 = ld4(p.w3c + base);
-            p1 = ld4(p.po + base);   p2 = ld4(p.pc + base);
-            w21 = ld4(p.w21 + base);
-        }
         if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) ok = false;
         while (ok && waited <= t + 2 * kRadius) {
             ok = pipe_wait(P, waited);
             if (ok) ++waited;
         }
+        ok = __all_sync(0xffffffffu, ok);   // keep warps converged for the shuffles below
         if (!ok) break;
+        bool amb[4] = {false, false, false, false};
+        float out[4], alt[4], m2v[4];
+        float a13[4] = {0.f, 0.f, 0.f, 0.f}, a21[4] = {0.f, 0.f, 0.f, 0.f};
+        float a33[4] = {0.f, 0.f, 0.f, 0.f}, a3[4] = {0.f, 0.f, 0.f, 0.f};
         if (row_ok) {
             float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
             quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
@@ -639,34 +671,30 @@ __global__ void __launch_bounds__(kThreads, 2)
                 // scalar operator, GPU_kernel.cu:93-111
                 float h2 = __fmul_rn(Ux[j], Ux[j]);
                 h2 = fmaf(Uy[j], Uy[j], h2);
-                float m2 = fmaf(Uz[j], Uz[j], h2);
-                float s = 1.0f;
-                float e2x = f4(Ev, j);
-                if (m2 > T2) {
-                    float aa = __fdiv_rn(h2, m2);
-                    float bb = __fsub_rn(1.0f, aa);
-                    float den = fmaf(e2x, aa, 1.0f);
-                    float num = __fmul_rn(__fmul_rn(f4(Rv, j), aa), bb);
-                    float qq = __fdiv_rn(num, __fmul_rn(den, den));
-                    s = fmaf(0.5f, __fsqrt_rn(__fsub_rn(1.0f, qq)), 0.5f);
-                }
-                e2[j] = __fadd_rn(1.0f, e2x);
+                const float m2 = fmaf(Uz[j], Uz[j], h2);
+                if (SPEC && cell_ok[j])
+                    mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+                const bool above = m2 > T2lo;
+                amb[j] = SPEC && cell_ok[j] && above && !(m2 > T2hi);
+                const float s = above ? aniso_s(h2, m2, f4(Ev, j), f4(Rv, j)) : 1.0f;
+                e2[j] = __fadd_rn(1.0f, f4(Ev, j));
                 KS[j] = __fmul_rn(f4(Kv, j), s);
+                m2v[j] = m2;
+                alt[j] = 0.0f;
             }
-            float out[4];
             if (!pml_quad) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
-                    out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
+                    const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
+                    const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
+                    out[j] = fmaf(KS[j], Lp, lin);
+                    if (SPEC && amb[j]) alt[j] = fmaf(f4(Kv, j), Lp, lin);
                 }
             } else {
-                if (!PREFETCH) {
-                    w11 = ld4(p.w1o + base); w12 = ld4(p.w1c + base);
-                    w31 = ld4(p.w3o + base); w32 = ld4(p.w3c + base);
-                    p1 = ld4(p.po + base);   p2 = ld4(p.pc + base);
-                    w21 = ld4(p.w21 + base);
-                }
+                const float4 w11 = ld4(p.w1o + base), w12 = ld4(p.w1c + base);
+                const float4 w31 = ld4(p.w3o + base), w32 = ld4(p.w3c + base);
+                const float4 p1 = ld4(p.po + base), p2 = ld4(p.pc + base);
+                const float4 w21 = ld4(p.w21o + base);
                 float n13[4], n21[4], n33[4], n3[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -674,10 +702,12 @@ __global__ void __launch_bounds__(kThreads, 2)
                     const int f = cell_ok[j] ? region_of(x, y, z, nx, ny, nz, pml) : -2;
                     n13[j] = 0.0f; n33[j] = 0.0f; n3[j] = 0.0f; n21[j] = f4(w21, j);
                     if (f == -2) {
-                        out[j] = f4(u1v, j);   // outside [5,n-5)^3: never updated
+                        out[j] = u0[j];   // outside [5,n-5)^3: never updated
                     } else if (f < 0) {
-                        float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
-                        out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
+                        const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
+                        const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
+                        out[j] = fmaf(KS[j], Lp, lin);
+                        if (SPEC && amb[j]) alt[j] = fmaf(f4(Kv, j), Lp, lin);
                     } else {
                         int li, pr;
                         switch (f) {
@@ -688,31 +718,41 @@ __global__ void __launch_bounds__(kThreads, 2)
                         case F_T: li = pml - z; pr = 2; break;
                         default: li = z - nz + pml; pr = 2; break;
                         }
-                        out[j] = pml_cell(f, tab[pr * pml + li], KS[j], e2[j], Ux[j], Uy[j], Uz[j],
-                                          Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
-                                          f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
-                                          n13[j], n21[j], n33[j], n3[j]);
+                        const float4 lc = tab[pr * pml + li];
+                        out[j] = pml_cell(f, lc, KS[j], e2[j], Ux[j], Uy[j], Uz[j], Uxx[j],
+                                          Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j), f4(w21, j),
+                                          f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j), n13[j],
+                                          n21[j], n33[j], n3[j]);
+                        if (SPEC && amb[j])
+                            alt[j] = pml_cell(f, lc, f4(Kv, j), e2[j], Ux[j], Uy[j], Uz[j], Uxx[j],
+                                              Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
+                                              f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
+                                              f4(p2, j), a13[j], a21[j], a33[j], a3[j]);
                     }
                 }
                 *reinterpret_cast<float4 *>(p.w1n + base) = make_float4(n13[0], n13[1], n13[2], n13[3]);
                 *reinterpret_cast<float4 *>(p.w3n + base) = make_float4(n33[0], n33[1], n33[2], n33[3]);
                 *reinterpret_cast<float4 *>(p.pn + base) = make_float4(n3[0], n3[1], n3[2], n3[3]);
-                *reinterpret_cast<float4 *>(p.w21 + base) = make_float4(n21[0], n21[1], n21[2], n21[3]);
+                *reinterpret_cast<float4 *>(p.w21n + base) = make_float4(n21[0], n21[1], n21[2], n21[3]);
             }
             // source injection (GPU_kernel.cu:727): u3 += source * wavelet
             for (int e = 0; e < ncsrc; ++e) {
                 const SrcEntry s = csrc[e];
                 if (s.z == z && s.x == x) {
-                    int j = s.y - yq;
+                    const int js = s.y - yq;
+                    const float add = __fmul_rn(s.v, p.wavelet);
 #pragma unroll
                     for (int jj = 0; jj < 4; ++jj)
-                        if (jj == j) out[jj] = __fadd_rn(out[jj], __fmul_rn(s.v, p.wavelet));
+                        if (jj == js) {
+                            out[jj] = __fadd_rn(out[jj], add);
+                            if (SPEC) alt[jj] = __fadd_rn(alt[jj], add);
+                        }
                 }
             }
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                if (!cell_ok[j]) out[j] = f4(u1v, j);
-            *reinterpret_cast<float4 *>(p.u_io + base) = make_float4(out[0], out[1], out[2], out[3]);
+                if (!cell_ok[j]) out[j] = u0[j];
+            *reinterpret_cast<float4 *>(p.u_out + base) = make_float4(out[0], out[1], out[2], out[3]);
             // receiver plane (3dPureqPModeling_single_shot.cu:333-337)
             if (p.record && z == p.sz && x >= pml && x < nx - pml) {
 #pragma unroll
@@ -723,14 +763,87 @@ __global__ void __launch_bounds__(kThreads, 2)
                 }
             }
         }
-        pipe_release(P, t);
-        if (PREFETCH) {
-            u1v = nu1; Kv = nK; Ev = nE; Rv = nR;
+        // alternatives of the uncertain cells, appended warp-wide (all lanes)
+        if (SPEC) {
+            const int cnt = (int)amb[0] + (int)amb[1] + (int)amb[2] + (int)amb[3];
+            if (__any_sync(0xffffffffu, cnt > 0)) {
+                int incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                unsigned wbase = 0;
+                if (lane == 31) wbase = atomicAdd(p.alt_count, (unsigned)total);
+                wbase = __shfl_sync(0xffffffffu, wbase, 31);
+                unsigned pos = wbase + (unsigned)(incl - cnt);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (!amb[j]) continue;
+                    if (pos < p.alt_cap) {
+                        AltEntry e;
+                        e.idx = (unsigned)(base + j);
+                        e.m2 = m2v[j];
+                        e.u3 = alt[j];
+                        const int f = region_of(x, yq + j, z, nx, ny, nz, pml);
+                        e.pml = (pml_quad && f >= 0) ? 1u : 0u;
+                        e.w13 = a13[j];
+                        e.p3 = a3[j];
+                        e.w21 = a21[j];
+                        e.w33 = a33[j];
+                        p.alt[pos] = e;
+                    }
+                    ++pos;
+                }
+            }
         }
+        pipe_release(P, t);
     }
     if (!ok) {
         atomicOr(p.err, kErrWaitTimeout);
         if (tid == 0) pipe_drain(P, next_issue);
+    }
+    if (SPEC) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0 && mx > 0.0f)
+            atomicMax(reinterpret_cast<unsigned *>(p.gmax + p.step), __float_as_uint(mx));
+    }
+}
+
+// Applies the alternatives of a speculative step, or requests its exact
+// re-run (*redo = 1) when the true max fell outside the window or the list
+// overflowed.  Also records the relative error of the prediction.
+__global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_err)
+{
+    const float M = p.gmax[p.step];
+    const float lo = p.win[0], hi = p.win[1], pred = p.win[2];
+    const unsigned n = *p.alt_count;
+    const bool inside = (M >= lo) && (M <= hi) && (n <= p.alt_cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *redo = inside ? 0 : 1;
+        *spec_err = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
+    }
+    if (!inside) return;
+    const float T2 = threshold_m2(M);
+    const int hy = p.ny - 2 * p.pml;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const AltEntry e = p.alt[i];
+        if (e.m2 > T2) continue;
+        p.u_out[e.idx] = e.u3;
+        if (e.pml) {
+            p.w1n[e.idx] = e.w13;
+            p.pn[e.idx] = e.p3;
+            p.w21n[e.idx] = e.w21;
+            p.w3n[e.idx] = e.w33;
+        }
+        if (p.record) {
+            const long long z = e.idx / p.plane, rem = e.idx % p.plane;
+            const int x = (int)(rem / p.ldy), y = (int)(rem % p.ldy);
+            if (z == p.sz && x >= p.pml && x < p.nx - p.pml && y >= p.pml && y < p.ny - p.pml)
+                p.record[(long long)(x - p.pml) * hy + (y - p.pml)] = e.u3;
+        }
     }
 }
 
@@ -825,7 +938,8 @@ cudaError_t configure_kernels()
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-static inline int plane_threads(int tile_x) { return kQuadsY * tile_x; }
+// whole warps: rows past tile_x are idle, so every warp collective sees 32 lanes
+static inline int plane_threads(int tile_x) { return (kQuadsY * tile_x + 31) & ~31; }
 
 cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
                            cudaStream_t stream, int variant)
@@ -840,10 +954,18 @@ cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 g
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
                         cudaStream_t stream, int variant)
 {
-    if (variant == 0)
-        qp3d_step_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
-    else
+    if (p.spec)
         qp3d_step_kernel<true><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+    else
+        qp3d_step_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+    (void)variant;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
+                         int nsm)
+{
+    qp3d_fixup_kernel<<<2 * nsm, 256, 0, stream>>>(p, redo, spec_err);
     return cudaGetLastError();
 }
 

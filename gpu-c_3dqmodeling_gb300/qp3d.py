@@ -48,9 +48,9 @@ EXPORTS = [
     "qp3d_version", "qp3d_strerror", "qp3d_ctx_create", "qp3d_ctx_destroy",
     "qp3d_ctx_last_error", "qp3d_forward", "qp3d_shot_load", "qp3d_shot_reset",
     "qp3d_shot_advance", "qp3d_shot_sync", "qp3d_shot_step", "qp3d_shot_read_record",
-    "qp3d_shot_read_uxyzmax", "qp3d_shot_snapshot", "qp3d_pml_state_size",
+    "qp3d_shot_read_uxyzmax", "qp3d_shot_read_stats", "qp3d_shot_snapshot", "qp3d_pml_state_size",
     "qp3d_shot_write_state", "qp3d_shot_read_state", "qp3d_shot_time",
-    "qp3d_shot_launches_per_step", "qp3d_tune", "qp3d_tune_get", "qp3d_event_record",
+    "qp3d_shot_launches_per_step", "qp3d_ctx_launch_count", "qp3d_tune", "qp3d_tune_get", "qp3d_event_record",
     "qp3d_event_elapsed",
     "qp3d_host_alloc", "qp3d_host_free", "qp3d_fdcoff1", "qp3d_fdcoff2", "qp3d_pmlcoff",
     "qp3d_source", "qp3d_extend_model", "qp3d_absmax", "qp3d_readmodel3d",
@@ -82,6 +82,7 @@ def load():
         "qp3d_shot_step": (ctypes.c_int, [_vp]),
         "qp3d_shot_read_record": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp]),
         "qp3d_shot_read_uxyzmax": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp]),
+        "qp3d_shot_read_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
         "qp3d_shot_snapshot": (ctypes.c_int, [_vp, P(Snap)]),
         "qp3d_pml_state_size": (ctypes.c_size_t, [ctypes.c_int] * 4),
         "qp3d_shot_write_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp]),
@@ -89,6 +90,7 @@ def load():
         "qp3d_shot_time": (ctypes.c_int, [_vp, ctypes.c_int, P(ctypes.c_float),
                                           P(ctypes.c_float), P(ctypes.c_float)]),
         "qp3d_shot_launches_per_step": (ctypes.c_int, [_vp]),
+        "qp3d_ctx_launch_count": (ctypes.c_longlong, [_vp]),
         "qp3d_tune": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
         "qp3d_tune_get": (ctypes.c_int, [_vp, ctypes.c_char_p]),
         "qp3d_event_record": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -307,6 +309,15 @@ class Context:
         self._check(self._L.qp3d_shot_read_uxyzmax(self.h, k0, n, _p(out)), "read_uxyzmax")
         return out
 
+    def stats(self, k0=0, n=None):
+        """(redo flags, alternatives count) per step."""
+        if n is None:
+            n = self.step - k0
+        redo = np.zeros(n, np.int32)
+        alt = np.zeros(n, np.uint32)
+        self._check(self._L.qp3d_shot_read_stats(self.h, k0, n, _p(redo), _p(alt)), "read_stats")
+        return redo, alt
+
     def write_state(self, step, u_prev=None, u_cur=None, pml=None):
         f = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
         u_prev, u_cur, pml = f(u_prev), f(u_cur), f(pml)
@@ -341,6 +352,9 @@ class Context:
 
     def launches_per_step(self):
         return int(self._L.qp3d_shot_launches_per_step(self.h))
+
+    def launch_count(self):
+        return int(self._L.qp3d_ctx_launch_count(self.h))
 
     def tune(self, **kv):
         for key, value in kv.items():

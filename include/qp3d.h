@@ -117,13 +117,25 @@ int qp3d_shot_write_state(qp3d_ctx *ctx, int step, const float *u_prev,
 int qp3d_shot_read_state(qp3d_ctx *ctx, float *u_prev, float *u_cur,
                          float *pml_state);
 
+/* Threshold bookkeeping of steps [k0, k0+nsteps): redo[i] = 1 when the
+ * step's predicted max window missed and the step was re-run exactly;
+ * alt[i] = number of cells whose decision waited for the exact max.
+ * Steps computed with the gradmax pre-pass report 0 for both. */
+int qp3d_shot_read_stats(qp3d_ctx *ctx, int k0, int nsteps, int *redo,
+                         unsigned *alt);
+
 /* Device timing of nsteps further steps with CUDA events on the context's
- * stream.  ms_total: whole interval; ms_step / ms_gradmax: sums of the
- * per-launch durations of the two kernels (NULL to skip per-kernel events). */
+ * stream.  ms_total: whole interval; ms_step: sum of the fused step kernel's
+ * launch durations; ms_gradmax: sum of the threshold overhead per step (the
+ * gradmax pre-pass, or the fix-up and gated re-run of a speculative step).
+ * NULL per-kernel pointers skip the per-kernel events. */
 int qp3d_shot_time(qp3d_ctx *ctx, int nsteps, float *ms_total, float *ms_step,
                    float *ms_gradmax);
-/* Number of kernels the library launches per time step for the loaded shot. */
+/* Number of kernels the library launches per time step for the loaded shot
+ * at its current step, and the total number of kernels this context has
+ * launched since it was created. */
 int qp3d_shot_launches_per_step(const qp3d_ctx *ctx);
+long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
 
 /* Launch tuning (autotuner hook).  Keys: "step_variant" (0: loads at use,
  * 1: next-plane prefetch), "gradmax_variant" (0: shared-memory z taps,

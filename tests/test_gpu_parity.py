@@ -245,21 +245,46 @@ def test_timing_helper(ctx):
     assert ms_step + ms_grad <= total * 1.05 + 0.05
 
 
-@pytest.mark.parametrize("step_v,grad_v,tile_x,chunks", [(0, 0, 0, 0), (1, 1, 0, 0),
-                                                         (1, 0, 17, 3), (0, 1, 32, 1),
-                                                         (1, 1, 9, 5)])
-def test_tuning_settings_are_bit_identical(ctx, step_v, grad_v, tile_x, chunks):
-    """Every launch variant, tile height and z-chunking computes the same bits
-    as the oracle mirror (the autotuner may pick any of them)."""
+@pytest.mark.parametrize("mode,grad_v,tile_x,chunks", [(0, 0, 0, 0), (1, 1, 0, 0),
+                                                       (1, 0, 17, 3), (0, 1, 32, 1),
+                                                       (1, 1, 9, 5)])
+def test_tuning_settings_are_bit_identical(ctx, mode, grad_v, tile_x, chunks):
+    """Every threshold mode, launch variant, tile height and z-chunking
+    computes the same bits as the oracle mirror (the autotuner may pick any)."""
     shot = synthetic.small_case(hx=30, hy=34, nz0=40, pml=8, nt=30, seed=12)
-    ctx.tune(step_variant=step_v, gradmax_variant=grad_v, tile_x=tile_x, chunks=chunks)
+    ctx.tune(threshold_mode=mode, gradmax_variant=grad_v, tile_x=tile_x, chunks=chunks)
     try:
         rec = ctx.forward(shot)
         ctx.load(shot)
         ctx.advance(shot.nt)
         mx = ctx.uxyzmax()
     finally:
-        ctx.tune(step_variant=1, gradmax_variant=1, tile_x=0, chunks=0)
+        ctx.tune(threshold_mode=1, gradmax_variant=0, tile_x=0, chunks=0)
     mrec, mmx, _ = O.run(O.MIRROR, shot.to_oracle(O))
     assert bits_equal(rec, mrec)
     assert bits_equal(mx, mmx)
+
+
+@pytest.mark.parametrize("delta_ppm,alt_cap", [(0, 0), (250000, 0), (5000, 1), (5000, 0)])
+def test_speculative_threshold_paths(ctx, delta_ppm, alt_cap):
+    """The speculative step: a window of zero width forces exact re-runs, a
+    wide one fills the alternatives list, a one-entry list overflows into
+    re-runs; every path stays bit-identical to the mirror."""
+    shot = synthetic.small_case(hx=26, hy=30, nz0=30, pml=8, nt=90, seed=21)
+    ctx.tune(spec_delta_ppm=delta_ppm, alt_cap=alt_cap)
+    try:
+        ctx.load(shot)
+        ctx.advance(shot.nt)
+        rec, mx = ctx.record(), ctx.uxyzmax()
+        redo, alt = ctx.stats()
+    finally:
+        ctx.tune(spec_delta_ppm=5000, alt_cap=0)
+    mrec, mmx, _ = O.run(O.MIRROR, shot.to_oracle(O))
+    assert bits_equal(rec, mrec)
+    assert bits_equal(mx, mmx)
+    if alt_cap == 1:
+        assert redo[3:].sum() > 0
+    if delta_ppm == 250000:
+        assert alt.max() > 0
+    print("delta %d cap %d: re-runs %d of %d, max alternatives %d" % (
+        delta_ppm, alt_cap, int(redo.sum()), shot.nt, int(alt.max())))
