@@ -78,7 +78,7 @@ struct qp3d_ctx {
     // tuning
     int step_variant = 0, gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
     int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
-    float delta_min = 0.005f;        // smallest half-width of the predicted window
+    float delta_min = 0.02f;         // smallest half-width of the predicted window
     unsigned tune_alt_cap = 0;
     long long launches = 0;          // kernels launched by this context
 };
@@ -255,7 +255,7 @@ static void plan_launch(qp3d_ctx *ctx)
     ctx->nyt = (g.ny - kRadius - 1) / kTileY + 1;   // last tile starts below ny-5
     int ncz = g.nz - 2 * kRadius;
     long long tiles = (long long)ctx->nxt * ctx->nyt;
-    long long target = 6ll * ctx->nsm;               // ~3 waves at 2 CTAs/SM
+    long long target = 18ll * ctx->nsm;              // ~9 waves at 2 CTAs/SM
     int nch = (int)((target + tiles - 1) / tiles);
     int maxch = std::max(1, ncz / 24);
     nch = std::max(1, std::min(nch, maxch));
@@ -332,7 +332,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         CK(cudaMalloc(&ctx->alt_count, ntb * sizeof(unsigned)));
         CK(cudaMalloc(&ctx->spec_err, sizeof(float)));
         long long cap = ctx->tune_alt_cap ? (long long)ctx->tune_alt_cap
-                                          : std::max(1ll << 20, ctx->vol / 16);
+                                          : std::max(1ll << 20, ctx->vol / 4);
         ctx->alt_cap = (unsigned)std::min(cap, (long long)0x7fffffff);
         CK(cudaMalloc(&ctx->alt, (size_t)ctx->alt_cap * sizeof(AltEntry)));
     }
@@ -878,7 +878,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
             CK(cudaStreamSynchronize(ctx->stream));
             if (ctx->alt) cudaFree(ctx->alt);
             ctx->alt = nullptr;
-            long long cap = value ? (long long)value : std::max(1ll << 20, ctx->vol / 16);
+            long long cap = value ? (long long)value : std::max(1ll << 20, ctx->vol / 4);
             ctx->alt_cap = (unsigned)std::min(cap, (long long)0x7fffffff);
             CK(cudaMalloc(&ctx->alt, (size_t)std::max(ctx->alt_cap, 1u) * sizeof(AltEntry)));
         }

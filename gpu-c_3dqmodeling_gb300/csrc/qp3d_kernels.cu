@@ -554,9 +554,10 @@ __device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &p
     float r = (m0 > 0.0f) ? __fdiv_rn(m1, m0) : 1.0f;
     r = fminf(fmaxf(r, 0.5f), 2.0f);
     pred = __fmul_rn(m1, r);
+    // cover both "the max keeps its trend" and "the max stays where it was"
     const float d = fminf(0.25f, fmaxf(p.delta_min, __fmul_rn(3.0f, *p.spec_err)));
-    lo = __fmul_rn(pred, __fsub_rn(1.0f, d));
-    hi = __fmul_rn(pred, __fadd_rn(1.0f, d));
+    lo = __fmul_rn(fminf(pred, m1), __fsub_rn(1.0f, d));
+    hi = __fmul_rn(fmaxf(pred, m1), __fadd_rn(1.0f, d));
 }
 
 // S of one cell (GPU_kernel.cu:100-111), given it is above the threshold.

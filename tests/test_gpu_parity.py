@@ -265,7 +265,7 @@ def test_tuning_settings_are_bit_identical(ctx, mode, grad_v, tile_x, chunks):
     assert bits_equal(mx, mmx)
 
 
-@pytest.mark.parametrize("delta_ppm,alt_cap", [(0, 0), (250000, 0), (5000, 1), (5000, 0)])
+@pytest.mark.parametrize("delta_ppm,alt_cap", [(0, 0), (250000, 0), (20000, 1), (20000, 0)])
 def test_speculative_threshold_paths(ctx, delta_ppm, alt_cap):
     """The speculative step: a window of zero width forces exact re-runs, a
     wide one fills the alternatives list, a one-entry list overflows into
@@ -278,7 +278,7 @@ def test_speculative_threshold_paths(ctx, delta_ppm, alt_cap):
         rec, mx = ctx.record(), ctx.uxyzmax()
         redo, alt = ctx.stats()
     finally:
-        ctx.tune(spec_delta_ppm=5000, alt_cap=0)
+        ctx.tune(spec_delta_ppm=20000, alt_cap=0)
     mrec, mmx, _ = O.run(O.MIRROR, shot.to_oracle(O))
     assert bits_equal(rec, mrec)
     assert bits_equal(mx, mmx)
