@@ -38,6 +38,17 @@ void derive_coefs(const float *c, const float *c2, float dx, float dy, float dz,
     k->kx = -(2.0f * sx);
     k->ky = -(2.0f * sy);
     k->kz = -(2.0f * sz);
+    for (int m = 0; m < kRadius; m++) {
+        k->cx2[m] = make_float2(k->cx[m], k->cx[m]);
+        k->cy2[m] = make_float2(k->cy[m], k->cy[m]);
+        k->cz2[m] = make_float2(k->cz[m], k->cz[m]);
+        k->c2x2[m] = make_float2(k->c2x[m], k->c2x[m]);
+        k->c2y2[m] = make_float2(k->c2y[m], k->c2y[m]);
+        k->c2z2[m] = make_float2(k->c2z[m], k->c2z[m]);
+    }
+    k->kx2 = make_float2(k->kx, k->kx);
+    k->ky2 = make_float2(k->ky, k->ky);
+    k->kz2 = make_float2(k->kz, k->kz);
 }
 
 // Per-layer PML recursion coefficients (GPU_kernel.cu:569-572):

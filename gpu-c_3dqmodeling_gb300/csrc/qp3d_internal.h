@@ -39,6 +39,10 @@ struct Coefs {
     float cx[kRadius], cy[kRadius], cz[kRadius];      // c[31+m]/h
     float c2x[kRadius], c2y[kRadius], c2z[kRadius];   // c2[31+m]/h^2
     float kx, ky, kz;                                  // -2*sum(c2?)
+    // the same values duplicated in both lanes, for the paired FP32x2 stencil
+    float2 cx2[kRadius], cy2[kRadius], cz2[kRadius];
+    float2 c2x2[kRadius], c2y2[kRadius], c2z2[kRadius];
+    float2 kx2, ky2, kz2;
 };
 
 // One source sample: padded coordinates and the amplitude.

@@ -191,15 +191,34 @@ __device__ __forceinline__ int region_of(int x, int y, int z, int nx, int ny, in
 
 // ---------------------------------------------------------------------------
 // Stencil over one quad: first and second derivatives along x, y, z of the
-// four cells (x, y..y+3, z) from the staged planes.
+// four cells (x, y..y+3, z) from the staged planes.  Cells (0,1) and (2,3)
+// are processed as pairs with the packed FP32x2 instructions (add/mul/fma
+// .rn.f32x2, round-to-nearest per lane, so every lane is bit-identical to
+// the scalar operation it replaces).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+
+// slot of staged plane (base + d), base already reduced modulo kRing
+__device__ __forceinline__ int slot_add(int s, int d)
+{
+    s += d;
+    if (s >= kRing) s -= kRing;
+    if (s < 0) s += kRing;
+    return s;
+}
+
 template <bool SECOND>
 __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_floats, int t, int rc,
                                             const Coefs &k, float Ux[4], float Uy[4],
                                             float Uz[4], float Uxx[4], float Uyy[4],
                                             float Uzz[4], float u0[4])
 {
-    const float *pc = ring + (size_t)((t + kRadius) % kRing) * slot_floats;
+    const int sc = (t + kRadius) % kRing;
+    const float *pc = ring + (size_t)sc * slot_floats;
     // y taps: columns c-8 .. c+11 of the centre plane
     float Y[20];
 #pragma unroll
@@ -208,59 +227,66 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
         Y[4 * b] = v.x; Y[4 * b + 1] = v.y; Y[4 * b + 2] = v.z; Y[4 * b + 3] = v.w;
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        float c0 = Y[8 + j];
-        u0[j] = c0;
-        float g = 0.0f, l = 0.0f;
-        if (SECOND) l = __fmul_rn(k.ky, c0);
+    for (int h = 0; h < 2; ++h) {
+        const int j0 = 2 * h, j1 = 2 * h + 1;
+        const float2 c0 = f2(Y[8 + j0], Y[8 + j1]);
+        u0[j0] = c0.x;
+        u0[j1] = c0.y;
+        float2 g = f2(0.0f, 0.0f), l = f2(0.0f, 0.0f);
+        if (SECOND) l = __fmul2_rn(k.ky2, c0);
 #pragma unroll
         for (int m = 0; m < kRadius; ++m) {
-            float a = Y[8 + j + m + 1], b = Y[8 + j - m - 1];
-            float d = __fsub_rn(a, b);
-            g = (m == 0) ? __fmul_rn(k.cy[0], d) : fmaf(k.cy[m], d, g);
-            if (SECOND) l = fmaf(k.c2y[m], __fadd_rn(a, b), l);
+            const float2 a = f2(Y[8 + j0 + m + 1], Y[8 + j1 + m + 1]);
+            const float2 b = f2(Y[8 + j0 - m - 1], Y[8 + j1 - m - 1]);
+            const float2 d = sub2(a, b);
+            g = (m == 0) ? __fmul2_rn(k.cy2[0], d) : __ffma2_rn(k.cy2[m], d, g);
+            if (SECOND) l = __ffma2_rn(k.c2y2[m], __fadd2_rn(a, b), l);
         }
-        Uy[j] = g;
-        if (SECOND) Uyy[j] = l;
+        Uy[j0] = g.x; Uy[j1] = g.y;
+        if (SECOND) { Uyy[j0] = l.x; Uyy[j1] = l.y; }
     }
     // x taps: rows r +- m of the centre plane
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        Ux[j] = 0.0f;
-        if (SECOND) Uxx[j] = __fmul_rn(k.kx, u0[j]);
+    float2 gx[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, lx[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
+    if (SECOND) {
+        lx[0] = __fmul2_rn(k.kx2, f2(u0[0], u0[1]));
+        lx[1] = __fmul2_rn(k.kx2, f2(u0[2], u0[3]));
     }
 #pragma unroll
     for (int m = 0; m < kRadius; ++m) {
-        float4 a = lds4(pc + rc + (m + 1) * kBoxY);
-        float4 b = lds4(pc + rc - (m + 1) * kBoxY);
+        const float4 a = lds4(pc + rc + (m + 1) * kBoxY);
+        const float4 b = lds4(pc + rc - (m + 1) * kBoxY);
+        const float2 a2[2] = {f2(a.x, a.y), f2(a.z, a.w)}, b2[2] = {f2(b.x, b.y), f2(b.z, b.w)};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float av = f4(a, j), bv = f4(b, j);
-            float d = __fsub_rn(av, bv);
-            Ux[j] = (m == 0) ? __fmul_rn(k.cx[0], d) : fmaf(k.cx[m], d, Ux[j]);
-            if (SECOND) Uxx[j] = fmaf(k.c2x[m], __fadd_rn(av, bv), Uxx[j]);
+        for (int h = 0; h < 2; ++h) {
+            const float2 d = sub2(a2[h], b2[h]);
+            gx[h] = (m == 0) ? __fmul2_rn(k.cx2[0], d) : __ffma2_rn(k.cx2[m], d, gx[h]);
+            if (SECOND) lx[h] = __ffma2_rn(k.c2x2[m], __fadd2_rn(a2[h], b2[h]), lx[h]);
         }
     }
+    Ux[0] = gx[0].x; Ux[1] = gx[0].y; Ux[2] = gx[1].x; Ux[3] = gx[1].y;
+    if (SECOND) { Uxx[0] = lx[0].x; Uxx[1] = lx[0].y; Uxx[2] = lx[1].x; Uxx[3] = lx[1].y; }
     // z taps: planes t+5 +- m
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        Uz[j] = 0.0f;
-        if (SECOND) Uzz[j] = __fmul_rn(k.kz, u0[j]);
+    float2 gz[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, lz[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
+    if (SECOND) {
+        lz[0] = __fmul2_rn(k.kz2, f2(u0[0], u0[1]));
+        lz[1] = __fmul2_rn(k.kz2, f2(u0[2], u0[3]));
     }
 #pragma unroll
     for (int m = 0; m < kRadius; ++m) {
-        const float *pp = ring + (size_t)((t + kRadius + m + 1) % kRing) * slot_floats;
-        const float *pm = ring + (size_t)((t + kRadius - m - 1) % kRing) * slot_floats;
-        float4 a = lds4(pp + rc);
-        float4 b = lds4(pm + rc);
+        const float *pp = ring + (size_t)slot_add(sc, m + 1) * slot_floats;
+        const float *pm = ring + (size_t)slot_add(sc, -m - 1) * slot_floats;
+        const float4 a = lds4(pp + rc);
+        const float4 b = lds4(pm + rc);
+        const float2 a2[2] = {f2(a.x, a.y), f2(a.z, a.w)}, b2[2] = {f2(b.x, b.y), f2(b.z, b.w)};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float av = f4(a, j), bv = f4(b, j);
-            float d = __fsub_rn(av, bv);
-            Uz[j] = (m == 0) ? __fmul_rn(k.cz[0], d) : fmaf(k.cz[m], d, Uz[j]);
-            if (SECOND) Uzz[j] = fmaf(k.c2z[m], __fadd_rn(av, bv), Uzz[j]);
+        for (int h = 0; h < 2; ++h) {
+            const float2 d = sub2(a2[h], b2[h]);
+            gz[h] = (m == 0) ? __fmul2_rn(k.cz2[0], d) : __ffma2_rn(k.cz2[m], d, gz[h]);
+            if (SECOND) lz[h] = __ffma2_rn(k.c2z2[m], __fadd2_rn(a2[h], b2[h]), lz[h]);
         }
     }
+    Uz[0] = gz[0].x; Uz[1] = gz[0].y; Uz[2] = gz[1].x; Uz[3] = gz[1].y;
+    if (SECOND) { Uzz[0] = lz[0].x; Uzz[1] = lz[0].y; Uzz[2] = lz[1].x; Uzz[3] = lz[1].y; }
 }
 
 // ---------------------------------------------------------------------------
