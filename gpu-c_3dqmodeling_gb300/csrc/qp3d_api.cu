@@ -9,7 +9,7 @@
 // by the step kernel, and nothing crosses the host link inside the time loop
 // except optional snapshots.
 #include "qp3d_internal.h"
-#include "../../include/qp3d.h"
+#include "qp3d.h"
 
 #include <algorithm>
 #include <cstdarg>

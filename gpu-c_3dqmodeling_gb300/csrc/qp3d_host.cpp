@@ -5,8 +5,8 @@
 // Compiled with -ffp-contract=off: the derivations below state each float
 // rounding, and the CPU oracle's mirror variant derives the same tables the
 // same way, so kernel results can be compared bit for bit.
-#include "../../include/qp3d.h"
-#include "../../include/qp3d_modeling3d.h"
+#include "qp3d.h"
+#include "qp3d_modeling3d.h"
 #include "qp3d_internal.h"
 
 #include <cmath>
