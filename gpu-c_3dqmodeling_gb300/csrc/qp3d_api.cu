@@ -453,6 +453,7 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.dt = g.dt;
     p.step = k;
     p.wavelet = ctx->wavelet[k];
+    p.u_cur = ctx->U[a];
     p.u_prev = ctx->U[b];
     p.u_out = ctx->U[c];
     p.prm_k = ctx->K; p.prm_e = ctx->E2; p.prm_r = ctx->R8;

@@ -51,13 +51,12 @@ struct SrcEntry {
     float v;
 };
 
-// One cell whose threshold decision depended on the exact max: its u(k+1)
-// (and PML state) computed with S = 1, to be used if m2 <= T2(max).
+// One cell whose threshold decision waited for the exact max of the step.
 struct AltEntry {
     unsigned idx;        // pitched cell index
     float m2;            // |grad u|^2 as the kernel computed it
-    float u3, w13, p3, w21, w33;
-    unsigned pml;        // 1: the state alternatives are valid
+    float src;           // source term added to the cell (flags bit 0)
+    unsigned flags;
 };
 
 struct PlaneParams {
@@ -70,7 +69,9 @@ struct PlaneParams {
     float dt;
     int step;            // time step index k
     float wavelet;       // wavelet[k]
-    // wavefields: u(k) is staged by TMA; u(k-1) read, u(k+1) written
+    // wavefields: u(k) is staged by TMA (and read directly by the fix-up);
+    // u(k-1) read, u(k+1) written
+    const float *u_cur;
     const float *u_prev;
     float *u_out;
     const float *prm_k, *prm_e, *prm_r;

@@ -522,7 +522,9 @@ __global__ void __launch_bounds__(kThreads, 2)
 
 // ---------------------------------------------------------------------------
 // PML update of one cell (GPU_kernel.cu:566-637 restated with per-layer
-// coefficients a1 = (d*dt+1)^2-3, a2 = 2*d*dt-1, a3 = 1-dt*d).
+// coefficients a1 = (d*dt+1)^2-3, a2 = 2*d*dt-1, a3 = 1-dt*d).  Face codes
+// L=0 R=1 F=2 Bk=3 T=4 Bo=5; the odd faces take the minus sign on the
+// dd*u_n term.  Written with selects only.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float pml_cell(int f, float4 lc, float KS, float e2, float Ux,
                                           float Uy, float Uz, float Uxx, float Uyy, float Uzz,
@@ -530,17 +532,17 @@ __device__ __forceinline__ float pml_cell(int f, float4 lc, float KS, float e2, 
                                           float w32, float p1, float p2, float &nw13,
                                           float &nw21, float &nw33, float &np3)
 {
-    const bool isx = (f == F_L || f == F_R), isy = (f == F_F || f == F_BK);
+    const bool isx = f < 2, isz = f >= 4;
     const float e2KS = __fmul_rn(e2, KS);
-    const float A = (isx || isy) ? e2KS : KS;
-    const float Unn = isx ? Uxx : (isy ? Uyy : Uzz);
-    const float Un = isx ? Ux : (isy ? Uy : Uz);
-    const float Bt = (isx || isy) ? KS : e2KS;
-    const float Tt = isx ? fmaf(e2, Uyy, Uzz) : (isy ? fmaf(e2, Uxx, Uzz) : __fadd_rn(Uxx, Uyy));
+    const float A = isz ? KS : e2KS;
+    const float Unn = isx ? Uxx : (isz ? Uzz : Uyy);
+    const float Un = isx ? Ux : (isz ? Uz : Uy);
+    const float Bt = isz ? e2KS : KS;
+    const float Tt = isz ? __fadd_rn(Uxx, Uyy) : fmaf(e2, isx ? Uyy : Uxx, Uzz);
     const float a1 = lc.x, a2 = lc.y, a3 = lc.z, dd = lc.w;
     nw13 = fmaf(A, Unn, fmaf(-a1, w12, __fmul_rn(a2, w11)));
     float Ad = __fmul_rn(A, dd);
-    if (f == F_R || f == F_BK || f == F_BO) Ad = -Ad;
+    Ad = (f & 1) ? -Ad : Ad;
     np3 = fmaf(Ad, Un, fmaf(-a1, p2, __fmul_rn(a2, p1)));
     nw21 = fmaf(dt, np3, __fmul_rn(a3, w21));
     nw33 = fmaf(Bt, Tt, fmaf(2.0f, w32, -w31));
@@ -557,6 +559,15 @@ __device__ __forceinline__ float4 ld4(const float *p)
     return *reinterpret_cast<const float4 *>(p);
 }
 
+// Face code and layer index of a cell from its x/y/z face parts (-1: none),
+// in the reference's priority order.
+__device__ __forceinline__ void cell_face(int fx, int lix, int fy, int liy, int fz, int liz,
+                                          int &f, int &li)
+{
+    f = fx >= 0 ? fx : (fy >= 0 ? fy : fz);
+    li = fx >= 0 ? lix : (fy >= 0 ? liy : liz);
+}
+
 // ---------------------------------------------------------------------------
 // step kernel.
 //   SPEC = false ("exact"): the threshold comes from gmax[step], already
@@ -565,12 +576,13 @@ __device__ __forceinline__ float4 ld4(const float *p)
 //     speculation failed).
 //   SPEC = true: the max of the step is not known yet.  It is predicted from
 //     the two previous steps with a window [M_lo, M_hi]; a cell whose m2 lies
-//     in (T2(M_lo), T2(M_hi)] has an uncertain decision and is computed both
-//     ways -- the S = 1 result goes to the alternatives list -- and the
-//     kernel reduces the true max of the step into gmax[step] on the way.
-//     qp3d_fixup_kernel then applies the alternatives, or asks for the exact
-//     re-run when the max fell outside the window or the list overflowed.
-//   Both modes write bit-identical results.
+//     in (T2(M_lo), T2(M_hi)] has an uncertain decision: the kernel computes
+//     it as "above" and appends (cell, m2) to a list, and reduces the true max
+//     of the step into gmax[step] on the way.  qp3d_fixup_kernel then
+//     recomputes the listed cells that turn out to be below the threshold,
+//     or asks for the exact re-run when the max fell outside the window or
+//     the list overflowed.  The step never overwrites its inputs, so both
+//     are possible.  Both modes write bit-identical results.
 // ---------------------------------------------------------------------------
 __device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &pred)
 {
@@ -658,7 +670,19 @@ __global__ void __launch_bounds__(kThreads, 2)
 #pragma unroll
     for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < ny - kRadius);
     const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
-    const bool xy_interior = (x >= pml) && (x < nx - pml) && (yq >= pml) && (yq + 3 < ny - pml);
+    // x and y face parts, constant along z
+    const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
+    const int lix = x < pml ? pml - x : x - nx + pml;
+    int fy[4], liy[4];
+    bool any_fy = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int y = yq + j;
+        fy[j] = y < pml ? 2 : (y >= ny - pml ? 3 : -1);
+        liy[j] = y < pml ? pml - y : y - ny + pml;
+        any_fy = any_fy || (cell_ok[j] && fy[j] >= 0);
+    }
+    const bool xy_face = row_ok && (fx >= 0 || any_fy);
     const int hy = ny - 2 * pml;
     const Coefs &k = p.k;
     const float dt = p.dt;
@@ -670,6 +694,9 @@ __global__ void __launch_bounds__(kThreads, 2)
     long long base = (long long)z0 * p.plane + (long long)x * p.ldy + yq;
     for (int t = 0; t < nzc; ++t, base += p.plane) {
         const int z = z0 + t;
+        const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
+        const int liz = z < pml ? pml - z : z - nz + pml;
+        const bool pml_quad = xy_face || (row_ok && fz >= 0);
         float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
         if (row_ok) {
             u1v = ldg4(p.u_prev + base);
@@ -677,108 +704,101 @@ __global__ void __launch_bounds__(kThreads, 2)
             Ev = ldg4(p.prm_e + base);
             Rv = ldg4(p.prm_r + base);
         }
-        const bool pml_quad = row_ok && !(xy_interior && z >= pml && z < nz - pml);
+        float4 w11 = zero4, w12 = zero4, w31 = zero4, w32 = zero4, p1 = zero4, p2 = zero4,
+               w21 = zero4;
+        if (pml_quad) {
+            w11 = ldg4(p.w1o + base); w12 = ldg4(p.w1c + base);
+            w31 = ldg4(p.w3o + base); w32 = ldg4(p.w3c + base);
+            p1 = ldg4(p.po + base);   p2 = ldg4(p.pc + base);
+            w21 = ldg4(p.w21o + base);
+        }
         if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) ok = false;
         while (ok && waited <= t + 2 * kRadius) {
             ok = pipe_wait(P, waited);
             if (ok) ++waited;
         }
-        ok = __all_sync(0xffffffffu, ok);   // keep warps converged for the shuffles below
+        ok = __all_sync(0xffffffffu, ok);   // warps stay converged for the collectives below
         if (!ok) break;
-        bool amb[4] = {false, false, false, false};
-        float out[4], alt[4], m2v[4];
-        float a13[4] = {0.f, 0.f, 0.f, 0.f}, a21[4] = {0.f, 0.f, 0.f, 0.f};
-        float a33[4] = {0.f, 0.f, 0.f, 0.f}, a3[4] = {0.f, 0.f, 0.f, 0.f};
-        if (row_ok) {
-            float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
-            quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
-            float e2[4], KS[4];
+        float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+        quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        // scalar operator, GPU_kernel.cu:93-111
+        float h2[4], m2[4];
+        bool above[4], amb[4];
+        bool any_above = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            h2[j] = fmaf(Uy[j], Uy[j], __fmul_rn(Ux[j], Ux[j]));
+            m2[j] = fmaf(Uz[j], Uz[j], h2[j]);
+            if (SPEC && cell_ok[j])
+                mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+            above[j] = m2[j] > T2lo;
+            amb[j] = SPEC && cell_ok[j] && above[j] && !(m2[j] > T2hi);
+            any_above = any_above || (row_ok && above[j]);
+        }
+        float KS[4], e2[4];
+        if (__any_sync(0xffffffffu, any_above)) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                // scalar operator, GPU_kernel.cu:93-111
-                float h2 = __fmul_rn(Ux[j], Ux[j]);
-                h2 = fmaf(Uy[j], Uy[j], h2);
-                const float m2 = fmaf(Uz[j], Uz[j], h2);
-                if (SPEC && cell_ok[j])
-                    mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
-                const bool above = m2 > T2lo;
-                amb[j] = SPEC && cell_ok[j] && above && !(m2 > T2hi);
-                const float s = above ? aniso_s(h2, m2, f4(Ev, j), f4(Rv, j)) : 1.0f;
-                e2[j] = __fadd_rn(1.0f, f4(Ev, j));
-                KS[j] = __fmul_rn(f4(Kv, j), s);
-                m2v[j] = m2;
-                alt[j] = 0.0f;
+                const float s = aniso_s(h2[j], m2[j], f4(Ev, j), f4(Rv, j));
+                KS[j] = __fmul_rn(f4(Kv, j), above[j] ? s : 1.0f);
             }
-            if (!pml_quad) {
+        } else {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
-                    const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
-                    out[j] = fmaf(KS[j], Lp, lin);
-                    if (SPEC && amb[j]) alt[j] = fmaf(f4(Kv, j), Lp, lin);
-                }
-            } else {
-                const float4 w11 = ld4(p.w1o + base), w12 = ld4(p.w1c + base);
-                const float4 w31 = ld4(p.w3o + base), w32 = ld4(p.w3c + base);
-                const float4 p1 = ld4(p.po + base), p2 = ld4(p.pc + base);
-                const float4 w21 = ld4(p.w21o + base);
-                float n13[4], n21[4], n33[4], n3[4];
+            for (int j = 0; j < 4; ++j) KS[j] = __fmul_rn(f4(Kv, j), 1.0f);
+        }
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int y = yq + j;
-                    const int f = cell_ok[j] ? region_of(x, y, z, nx, ny, nz, pml) : -2;
-                    n13[j] = 0.0f; n33[j] = 0.0f; n3[j] = 0.0f; n21[j] = f4(w21, j);
-                    if (f == -2) {
-                        out[j] = u0[j];   // outside [5,n-5)^3: never updated
-                    } else if (f < 0) {
-                        const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
-                        const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
-                        out[j] = fmaf(KS[j], Lp, lin);
-                        if (SPEC && amb[j]) alt[j] = fmaf(f4(Kv, j), Lp, lin);
-                    } else {
-                        int li, pr;
-                        switch (f) {
-                        case F_L: li = pml - x; pr = 0; break;
-                        case F_R: li = x - nx + pml; pr = 0; break;
-                        case F_F: li = pml - y; pr = 1; break;
-                        case F_BK: li = y - ny + pml; pr = 1; break;
-                        case F_T: li = pml - z; pr = 2; break;
-                        default: li = z - nz + pml; pr = 2; break;
-                        }
-                        const float4 lc = tab[pr * pml + li];
-                        out[j] = pml_cell(f, lc, KS[j], e2[j], Ux[j], Uy[j], Uz[j], Uxx[j],
-                                          Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j), f4(w21, j),
-                                          f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j), n13[j],
-                                          n21[j], n33[j], n3[j]);
-                        if (SPEC && amb[j])
-                            alt[j] = pml_cell(f, lc, f4(Kv, j), e2[j], Ux[j], Uy[j], Uz[j], Uxx[j],
-                                              Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
-                                              f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
-                                              f4(p2, j), a13[j], a21[j], a33[j], a3[j]);
-                    }
-                }
+        for (int j = 0; j < 4; ++j) e2[j] = __fadd_rn(1.0f, f4(Ev, j));
+        float out[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
+            out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
+        }
+        if (__any_sync(0xffffffffu, pml_quad)) {
+            float n13[4], n21[4], n33[4], n3[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int f, li;
+                cell_face(fx, lix, fy[j], liy[j], fz, liz, f, li);
+                const bool is_pml = pml_quad && cell_ok[j] && f >= 0;
+                const float4 lc = tab[is_pml ? (f >> 1) * pml + li : 0];
+                const float v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e2[j], Ux[j], Uy[j], Uz[j],
+                                         Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
+                                         f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
+                                         n13[j], n21[j], n33[j], n3[j]);
+                out[j] = is_pml ? v : out[j];
+                n13[j] = is_pml ? n13[j] : 0.0f;
+                n33[j] = is_pml ? n33[j] : 0.0f;
+                n3[j] = is_pml ? n3[j] : 0.0f;
+                n21[j] = is_pml ? n21[j] : f4(w21, j);
+            }
+            if (pml_quad) {
                 *reinterpret_cast<float4 *>(p.w1n + base) = make_float4(n13[0], n13[1], n13[2], n13[3]);
                 *reinterpret_cast<float4 *>(p.w3n + base) = make_float4(n33[0], n33[1], n33[2], n33[3]);
                 *reinterpret_cast<float4 *>(p.pn + base) = make_float4(n3[0], n3[1], n3[2], n3[3]);
                 *reinterpret_cast<float4 *>(p.w21n + base) = make_float4(n21[0], n21[1], n21[2], n21[3]);
             }
-            // source injection (GPU_kernel.cu:727): u3 += source * wavelet
-            for (int e = 0; e < ncsrc; ++e) {
-                const SrcEntry s = csrc[e];
-                if (s.z == z && s.x == x) {
-                    const int js = s.y - yq;
-                    const float add = __fmul_rn(s.v, p.wavelet);
+        }
+        // source injection (GPU_kernel.cu:727): u3 += source * wavelet
+        float sadd[4] = {0.f, 0.f, 0.f, 0.f};
+        unsigned sflag = 0;
+        for (int e = 0; e < ncsrc; ++e) {
+            const SrcEntry s = csrc[e];
+            if (s.z == z && s.x == x) {
+                const int js = s.y - yq;
+                const float add = __fmul_rn(s.v, p.wavelet);
 #pragma unroll
-                    for (int jj = 0; jj < 4; ++jj)
-                        if (jj == js) {
-                            out[jj] = __fadd_rn(out[jj], add);
-                            if (SPEC) alt[jj] = __fadd_rn(alt[jj], add);
-                        }
-                }
+                for (int jj = 0; jj < 4; ++jj)
+                    if (jj == js) {
+                        out[jj] = __fadd_rn(out[jj], add);
+                        sadd[jj] = add;
+                        sflag |= 1u << jj;
+                    }
             }
+        }
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (!cell_ok[j]) out[j] = u0[j];
+        for (int j = 0; j < 4; ++j) out[j] = cell_ok[j] ? out[j] : u0[j];   // never updated
+        if (row_ok) {
             *reinterpret_cast<float4 *>(p.u_out + base) = make_float4(out[0], out[1], out[2], out[3]);
             // receiver plane (3dPureqPModeling_single_shot.cu:333-337)
             if (p.record && z == p.sz && x >= pml && x < nx - pml) {
@@ -790,7 +810,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                 }
             }
         }
-        // alternatives of the uncertain cells, appended warp-wide (all lanes)
+        // uncertain cells, appended warp-wide (all lanes take part)
         if (SPEC) {
             const int cnt = (int)amb[0] + (int)amb[1] + (int)amb[2] + (int)amb[3];
             if (__any_sync(0xffffffffu, cnt > 0)) {
@@ -811,14 +831,9 @@ __global__ void __launch_bounds__(kThreads, 2)
                     if (pos < p.alt_cap) {
                         AltEntry e;
                         e.idx = (unsigned)(base + j);
-                        e.m2 = m2v[j];
-                        e.u3 = alt[j];
-                        const int f = region_of(x, yq + j, z, nx, ny, nz, pml);
-                        e.pml = (pml_quad && f >= 0) ? 1u : 0u;
-                        e.w13 = a13[j];
-                        e.p3 = a3[j];
-                        e.w21 = a21[j];
-                        e.w33 = a33[j];
+                        e.m2 = m2[j];
+                        e.src = sadd[j];
+                        e.flags = (sflag >> j) & 1u;
                         p.alt[pos] = e;
                     }
                     ++pos;
@@ -839,9 +854,39 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// Applies the alternatives of a speculative step, or requests its exact
-// re-run (*redo = 1) when the true max fell outside the window or the list
-// overflowed.  Also records the relative error of the prediction.
+// Derivatives of u at one cell from global memory, in the same operation
+// order as quad_derivs (and the oracle's mirror).
+__device__ void cell_derivs(const float *u, long long i, long long sx, long long sz,
+                            const Coefs &k, float &Ux, float &Uy, float &Uz, float &Uxx,
+                            float &Uyy, float &Uzz, float &u0)
+{
+    u0 = u[i];
+    float g[3], l[3];
+    const long long st[3] = {sx, 1, sz};
+    const float *cc[3] = {k.cx, k.cy, k.cz};
+    const float *c2[3] = {k.c2x, k.c2y, k.c2z};
+    const float kk[3] = {k.kx, k.ky, k.kz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g[a] = 0.0f;
+        l[a] = __fmul_rn(kk[a], u0);
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m) {
+            const float pa = u[i + (m + 1) * st[a]], pb = u[i - (m + 1) * st[a]];
+            const float d = __fsub_rn(pa, pb);
+            g[a] = (m == 0) ? __fmul_rn(cc[a][0], d) : fmaf(cc[a][m], d, g[a]);
+            l[a] = fmaf(c2[a][m], __fadd_rn(pa, pb), l[a]);
+        }
+    }
+    Ux = g[0]; Uy = g[1]; Uz = g[2];
+    Uxx = l[0]; Uyy = l[1]; Uzz = l[2];
+}
+
+// Resolves a speculative step.  If the true max lies in the window and the
+// list did not overflow, every listed cell that is below the true threshold
+// is recomputed with S = 1 from the step's (untouched) inputs; otherwise
+// *redo = 1 and the gated exact re-run recomputes the whole step.  Also
+// records the relative error of the prediction.
 __global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_err)
 {
     const float M = p.gmax[p.step];
@@ -854,23 +899,43 @@ __global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_er
     }
     if (!inside) return;
     const float T2 = threshold_m2(M);
-    const int hy = p.ny - 2 * p.pml;
+    const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml, hy = ny - 2 * pml;
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const AltEntry e = p.alt[i];
         if (e.m2 > T2) continue;
-        p.u_out[e.idx] = e.u3;
-        if (e.pml) {
-            p.w1n[e.idx] = e.w13;
-            p.pn[e.idx] = e.p3;
-            p.w21n[e.idx] = e.w21;
-            p.w3n[e.idx] = e.w33;
+        const long long idx = e.idx;
+        const int z = (int)(idx / p.plane);
+        const long long rem = idx % p.plane;
+        const int x = (int)(rem / p.ldy), y = (int)(rem % p.ldy);
+        float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
+        cell_derivs(p.u_cur, idx, p.ldy, p.plane, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        const float K = p.prm_k[idx];
+        const float KS = __fmul_rn(K, 1.0f);
+        const float e2 = __fadd_rn(1.0f, p.prm_e[idx]);
+        float out;
+        const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
+        const int fy = y < pml ? 2 : (y >= ny - pml ? 3 : -1);
+        const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
+        int f, li;
+        cell_face(fx, x < pml ? pml - x : x - nx + pml, fy, y < pml ? pml - y : y - ny + pml, fz,
+                  z < pml ? pml - z : z - nz + pml, f, li);
+        if (f < 0) {
+            const float Lp = fmaf(e2, __fadd_rn(Uxx, Uyy), Uzz);
+            out = fmaf(KS, Lp, fmaf(2.0f, u0, -p.u_prev[idx]));
+        } else {
+            float n13, n21, n33, n3;
+            out = pml_cell(f, p.layers[(f >> 1) * pml + li], KS, e2, Ux, Uy, Uz, Uxx, Uyy, Uzz,
+                           p.dt, p.w1o[idx], p.w1c[idx], p.w21o[idx], p.w3o[idx], p.w3c[idx],
+                           p.po[idx], p.pc[idx], n13, n21, n33, n3);
+            p.w1n[idx] = n13;
+            p.pn[idx] = n3;
+            p.w21n[idx] = n21;
+            p.w3n[idx] = n33;
         }
-        if (p.record) {
-            const long long z = e.idx / p.plane, rem = e.idx % p.plane;
-            const int x = (int)(rem / p.ldy), y = (int)(rem % p.ldy);
-            if (z == p.sz && x >= p.pml && x < p.nx - p.pml && y >= p.pml && y < p.ny - p.pml)
-                p.record[(long long)(x - p.pml) * hy + (y - p.pml)] = e.u3;
-        }
+        if (e.flags & 1u) out = __fadd_rn(out, e.src);
+        p.u_out[idx] = out;
+        if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
+            p.record[(long long)(x - pml) * hy + (y - pml)] = out;
     }
 }
 
