@@ -26,7 +26,6 @@ constexpr int kQuadsY = kTileY / 4;
 constexpr int kHaloY = 8;         // y halo rounded up to 16 bytes
 constexpr int kBoxY = kTileY + 2 * kHaloY;   // 48 floats per staged row
 constexpr int kPrefetch = 2;      // planes loaded ahead of use
-constexpr int kL2Ahead = 3;       // planes of per-cell data prefetched into L2
 constexpr int kRing = 2 * kRadius + 1 + kPrefetch;   // staged planes
 constexpr int kMaxTileX = 32;
 constexpr int kThreads = kQuadsY * kMaxTileX;        // 256

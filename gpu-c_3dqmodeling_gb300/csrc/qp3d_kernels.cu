@@ -110,12 +110,6 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
         : "memory");
 }
 
-// Bring `bytes` (multiple of 16, 16-byte aligned) of global memory into L2.
-__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
-{
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
 __device__ __forceinline__ float4 lds4(const float *p)
 {
     return *reinterpret_cast<const float4 *>(p);
@@ -698,30 +692,11 @@ __global__ void __launch_bounds__(kThreads, 2)
     bool ok = true;
     int waited = 0;
     long long base = (long long)z0 * p.plane + (long long)x * p.ldy + yq;
-    // one lane per row keeps the row's next planes of every read stream on
-    // their way into L2 (128 B = the tile row of one stream)
-    const long long row0 = (long long)x * p.ldy + y0;
-    const bool pf_lane = row_ok && q == 0;
-    const bool row_face = fx >= 0 || y0 < pml || y0 + kTileY > ny - pml;   // any x/y face cell
     for (int t = 0; t < nzc; ++t, base += p.plane) {
         const int z = z0 + t;
         const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
         const int liz = z < pml ? pml - z : z - nz + pml;
         const bool pml_quad = xy_face || (row_ok && fz >= 0);
-        if (pf_lane && t + kL2Ahead < nzc) {
-            const int zp = z + kL2Ahead;
-            const long long off = (long long)zp * p.plane + row0;
-            prefetch_l2(p.u_prev + off, 128);
-            prefetch_l2(p.prm_k + off, 128);
-            prefetch_l2(p.prm_e + off, 128);
-            prefetch_l2(p.prm_r + off, 128);
-            if (row_face || zp < pml || zp >= nz - pml) {
-                prefetch_l2(p.w1o + off, 128); prefetch_l2(p.w1c + off, 128);
-                prefetch_l2(p.w3o + off, 128); prefetch_l2(p.w3c + off, 128);
-                prefetch_l2(p.po + off, 128);  prefetch_l2(p.pc + off, 128);
-                prefetch_l2(p.w21o + off, 128);
-            }
-        }
         float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
         if (row_ok) {
             u1v = ldg4(p.u_prev + base);
