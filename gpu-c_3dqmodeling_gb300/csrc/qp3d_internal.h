@@ -55,8 +55,9 @@ struct SrcEntry {
 struct AltEntry {
     unsigned idx;        // pitched cell index
     float m2;            // |grad u|^2 as the kernel computed it
-    float src;           // source term added to the cell (flags bit 0)
-    unsigned flags;
+    float v;             // interior cell: its u(k+1) with S = 1 (source included);
+                         // PML cell: the source term added to it (flags bit 0)
+    unsigned flags;      // bit 0: source added, bit 1: PML cell (recomputed)
 };
 
 struct PlaneParams {

@@ -748,11 +748,14 @@ __global__ void __launch_bounds__(kThreads, 2)
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) e2[j] = __fadd_rn(1.0f, f4(Ev, j));
-        float out[4];
+        float out[4], alt[4];
+        bool cell_pml[4] = {false, false, false, false};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
-            out[j] = fmaf(KS[j], Lp, fmaf(2.0f, u0[j], -f4(u1v, j)));
+            const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
+            out[j] = fmaf(KS[j], Lp, lin);
+            alt[j] = fmaf(__fmul_rn(f4(Kv, j), 1.0f), Lp, lin);   // S = 1, for deferred cells
         }
         if (__any_sync(0xffffffffu, pml_quad)) {
             float n13[4], n21[4], n33[4], n3[4];
@@ -767,6 +770,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                                          f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
                                          n13[j], n21[j], n33[j], n3[j]);
                 out[j] = is_pml ? v : out[j];
+                cell_pml[j] = is_pml;
                 n13[j] = is_pml ? n13[j] : 0.0f;
                 n33[j] = is_pml ? n33[j] : 0.0f;
                 n3[j] = is_pml ? n3[j] : 0.0f;
@@ -791,6 +795,7 @@ __global__ void __launch_bounds__(kThreads, 2)
                 for (int jj = 0; jj < 4; ++jj)
                     if (jj == js) {
                         out[jj] = __fadd_rn(out[jj], add);
+                        alt[jj] = __fadd_rn(alt[jj], add);
                         sadd[jj] = add;
                         sflag |= 1u << jj;
                     }
@@ -832,8 +837,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                         AltEntry e;
                         e.idx = (unsigned)(base + j);
                         e.m2 = m2[j];
-                        e.src = sadd[j];
-                        e.flags = (sflag >> j) & 1u;
+                        e.v = cell_pml[j] ? sadd[j] : alt[j];
+                        e.flags = ((sflag >> j) & 1u) | (cell_pml[j] ? 2u : 0u);
                         p.alt[pos] = e;
                     }
                     ++pos;
@@ -907,6 +912,12 @@ __global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_er
         const int z = (int)(idx / p.plane);
         const long long rem = idx % p.plane;
         const int x = (int)(rem / p.ldy), y = (int)(rem % p.ldy);
+        if (!(e.flags & 2u)) {   // interior cell: its S = 1 value came with the entry
+            p.u_out[idx] = e.v;
+            if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
+                p.record[(long long)(x - pml) * hy + (y - pml)] = e.v;
+            continue;
+        }
         float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
         cell_derivs(p.u_cur, idx, p.ldy, p.plane, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
         const float K = p.prm_k[idx];
@@ -932,7 +943,7 @@ __global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_er
             p.w21n[idx] = n21;
             p.w3n[idx] = n33;
         }
-        if (e.flags & 1u) out = __fadd_rn(out, e.src);
+        if (e.flags & 1u) out = __fadd_rn(out, e.v);
         p.u_out[idx] = out;
         if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
             p.record[(long long)(x - pml) * hy + (y - pml)] = out;
@@ -1057,7 +1068,7 @@ cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid
 cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
                          int nsm)
 {
-    qp3d_fixup_kernel<<<2 * nsm, 256, 0, stream>>>(p, redo, spec_err);
+    qp3d_fixup_kernel<<<8 * nsm, 256, 0, stream>>>(p, redo, spec_err);
     return cudaGetLastError();
 }
 
