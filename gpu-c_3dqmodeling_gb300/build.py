@@ -26,6 +26,7 @@ CU_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 SOURCES = [
     ("qp3d_kernels.cu", [NVCC] + CU_FLAGS + ["-fmad=false"]),
     ("qp3d_api.cu", [NVCC] + CU_FLAGS),
+    ("qp3d_noalloc.cu", [NVCC] + CU_FLAGS),
     ("qp3d_host.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
                        "-Wall", "-I", INCLUDE, "-I", "/usr/local/cuda/include"]),
 ]

@@ -124,6 +124,10 @@ cudaError_t launch_params(const float *vp, const float *eps, const float *del,
                           float *K, float *E2, float *R8, long long n, float dt,
                           cudaStream_t stream);
 size_t plane_smem_bytes(int tile_x, int pml);
+cudaError_t configure_gradmax_partial();
+cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid,
+                                   size_t smem, cudaStream_t stream, float *partial,
+                                   unsigned nblocks, float *out);
 cudaError_t configure_kernels();
 
 }  // namespace qp3d

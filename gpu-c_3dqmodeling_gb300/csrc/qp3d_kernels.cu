@@ -521,6 +521,98 @@ __global__ void __launch_bounds__(kThreads, 2)
 }
 
 // ---------------------------------------------------------------------------
+// gradmax with per-CTA partial results: the same staging and arithmetic as
+// qp3d_gradmax_kernel<false>, but each CTA writes its own maximum to
+// partial[linear CTA index] (every CTA writes its slot, also when it has no
+// cell), for callers that supply the partial array themselves.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 2)
+    qp3d_gradmax_partial_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p,
+                                float *partial)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ float wmax[kThreads / 32];
+    const int tid = threadIdx.x;
+    const unsigned cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
+    const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
+    const int z0 = kRadius + blockIdx.z * p.chunk_z;
+    const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
+    if (z0 >= z1) {
+        if (tid == 0) partial[cta] = 0.0f;
+        return;
+    }
+    const int nzc = z1 - z0;
+    Pipe P;
+    pipe_setup(P, smem, p, y0, x0, z0, nzc);
+    int next_issue = 0;
+    if (tid == 0) {
+        pipe_init(P);
+        next_issue = min(kRing, P.nplanes);
+        for (int i = 0; i < next_issue; ++i) pipe_issue(P, &tm_u, i);
+    }
+    __syncthreads();
+    const int x = x0 + r, yq = y0 + 4 * q;
+    const bool row_ok = (r < p.tile_x) && (x < p.nx - kRadius);
+    bool cell_ok[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < p.ny - kRadius);
+    const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
+    float mx = 0.0f;
+    bool ok = true;
+    int waited = 0;
+    for (int t = 0; t < nzc; ++t) {
+        if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) ok = false;
+        while (ok && waited <= t + 2 * kRadius) {
+            ok = pipe_wait(P, waited);
+            if (ok) ++waited;
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
+        if (row_ok) {
+            float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+            quad_derivs<false>(P.ring, P.slot_floats, t, rc, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (cell_ok[j])
+                    mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+        }
+        pipe_release(P, t);
+    }
+    if (!ok) {
+        atomicOr(p.err, kErrWaitTimeout);
+        if (tid == 0) pipe_drain(P, next_issue);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0) wmax[tid / 32] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        float m = 0.0f;
+        for (int w = 0; w < (int)blockDim.x / 32; ++w) m = fmaxf(m, wmax[w]);
+        partial[cta] = m;
+    }
+}
+
+// One block: out[0] = max(partial[0..n)), or NaN when *err is set.
+__global__ void qp3d_reduce_max_kernel(const float *partial, unsigned n, const unsigned *err,
+                                       float *out)
+{
+    __shared__ float wmax[32];
+    float m = 0.0f;
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, partial[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x / 32] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = 0.0f;
+        for (int w = 0; w < (int)blockDim.x / 32; ++w) r = fmaxf(r, wmax[w]);
+        out[0] = (err && *err) ? __int_as_float(0x7fc00000) : r;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // PML update of one cell (GPU_kernel.cu:566-637 restated with per-layer
 // coefficients a1 = (d*dt+1)^2-3, a2 = 2*d*dt-1, a3 = 1-dt*d).  Face codes
 // L=0 R=1 F=2 Bk=3 T=4 Bo=5; the odd faces take the minus sign on the
@@ -1062,6 +1154,23 @@ cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid
     else
         qp3d_step_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
     (void)variant;
+    return cudaGetLastError();
+}
+
+cudaError_t configure_gradmax_partial()
+{
+    return cudaFuncSetAttribute(qp3d_gradmax_partial_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid,
+                                   size_t smem, cudaStream_t stream, float *partial,
+                                   unsigned nblocks, float *out)
+{
+    qp3d_gradmax_partial_kernel<<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    qp3d_reduce_max_kernel<<<1, 1024, 0, stream>>>(partial, nblocks, p.err, out);
     return cudaGetLastError();
 }
 

@@ -52,7 +52,7 @@ EXPORTS = [
     "qp3d_shot_write_state", "qp3d_shot_read_state", "qp3d_shot_time",
     "qp3d_shot_launches_per_step", "qp3d_ctx_launch_count", "qp3d_tune", "qp3d_tune_get", "qp3d_event_record",
     "qp3d_event_elapsed",
-    "qp3d_host_alloc", "qp3d_host_free", "qp3d_fdcoff1", "qp3d_fdcoff2", "qp3d_pmlcoff",
+    "qp3d_host_alloc", "qp3d_host_free", "qp3d_gradmax_noalloc", "qp3d_fdcoff1", "qp3d_fdcoff2", "qp3d_pmlcoff",
     "qp3d_source", "qp3d_extend_model", "qp3d_absmax", "qp3d_readmodel3d",
 ]
 
@@ -98,6 +98,10 @@ def load():
                                               P(ctypes.c_float)]),
         "qp3d_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
         "qp3d_host_free": (None, [_vp]),
+        "qp3d_gradmax_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                                ctypes.c_float, _vp, _vp, _vp, ctypes.c_char_p,
+                                                ctypes.c_size_t]),
         "qp3d_fdcoff1": (None, [_vp]),
         "qp3d_fdcoff2": (None, [_vp]),
         "qp3d_pmlcoff": (None, [ctypes.c_int] + [ctypes.c_float] * 4 + [_vp] * 6),

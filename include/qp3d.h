@@ -156,6 +156,29 @@ int qp3d_event_elapsed(qp3d_ctx *ctx, int slot_start, int slot_end, float *ms);
 void *qp3d_host_alloc(size_t bytes);
 void qp3d_host_free(void *p);
 
+/* max over [5,n-5)^3 of max(|du/dx|,|du/dy|,|du/dz|) of a wavefield the
+ * caller keeps in device memory, computed without allocating any device
+ * memory.  No counterpart in the reference (there the maximum is a host scan,
+ * 3dPureqPModeling_single_shot.cu:284-292); it serves callers that cannot let
+ * a library allocate: a framework that already holds the device memory, a
+ * loop that forbids allocation after start-up, or a CUDA graph being
+ * recorded, where cudaMalloc and cudaFree cannot be captured.
+ *   d_u    device pointer, [nz][nx][ldy] float32, 16-byte aligned,
+ *          ldy >= ny and a multiple of 4
+ *   c      host pointer to the 36-entry fdcoff1 table
+ *   d_max  device pointer to one float; NaN if a device wait timed out
+ *   stream cudaStream_t (NULL: legacy default stream); asynchronous
+ *   err    optional message buffer (NULL to skip)
+ * Limit: the grid may need at most 65536 tiles of 32x32 cells per z chunk
+ * (nx*ny up to about 64 M cells); larger grids return QP3D_ERR_ARG.
+ * Its scratch is a fixed device array that every GPU loading the library
+ * holds until exit and that all calls share: calls that overlap on the GPU
+ * race.  The first call on each device sets up the scratch addresses and the
+ * kernel attributes; make it before any stream capture. */
+int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, int ldy,
+                         float dx, float dy, float dz, const float *c,
+                         float *d_max, void *stream, char *err, size_t errlen);
+
 /* Host utilities, restating the reference's (see the list above). */
 void qp3d_fdcoff1(float *c);
 void qp3d_fdcoff2(float *c2);
