@@ -29,7 +29,11 @@ SOURCES = [
     ("qp3d_noalloc.cu", [NVCC] + CU_FLAGS),
     ("qp3d_host.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
                        "-Wall", "-I", INCLUDE, "-I", "/usr/local/cuda/include"]),
+    ("qp3d_driver.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
+                         "-Wall", "-I", INCLUDE, "-I", "/usr/local/cuda/include"]),
 ]
+MAIN = ("qp3d_main.cpp", ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE])
+EXE = os.path.join(HERE, "bin", "qp3d_modeling")
 HEADERS = ["qp3d_internal.h"]
 
 
@@ -63,6 +67,15 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed\n%s\n%s" % (r.stdout, r.stderr))
+    # the modeling program, linked against the library next to it
+    main_obj = _compile(MAIN, force)
+    if force or _newer(EXE, [main_obj, LIB]):
+        os.makedirs(os.path.dirname(EXE), exist_ok=True)
+        cmd = ["g++", "-o", EXE, main_obj, "-L", os.path.dirname(LIB), "-lqp3d",
+               "-Wl,-rpath,$ORIGIN/../lib"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link of qp3d_modeling failed\n%s\n%s" % (r.stdout, r.stderr))
     if verbose:
         print(LIB)
     return LIB

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace qp3d {
@@ -181,29 +182,29 @@ extern "C" int qp3d_readmodel3d(const char *filename, float *a, int ny, int nx, 
 // ---------------------------------------------------------------------------
 // modeling3d drop-in (C++ linkage, 3dPureqPModeling_single_shot.h:4-6)
 // ---------------------------------------------------------------------------
-namespace {
+namespace qp3d {
 
-struct SnapFiles {
-    const char *prefix;
-};
-
-int write_raw(const char *name, const float *d, size_t n)
-{   // read_write.c:29-52 ("wb+", raw native floats)
+// Snapshot files named as 3dPureqPModeling_single_shot.cu:342-345
+// (<prefix><k>.dat and <prefix>_xz/_yz/_xy<k>.dat, raw native floats,
+// read_write.c:29-52); user points to the prefix (std::string).
+int write_snapshot_files(void *user, int step, int kind, const float *data, int n0, int n1,
+                         int n2)
+{
+    const std::string *prefix = static_cast<const std::string *>(user);
+    static const char *suffix[4] = {"", "_xz", "_yz", "_xy"};
+    if (kind < 0 || kind > 3) return -1;
+    char name[1024];
+    snprintf(name, sizeof(name), "%s%s%d.dat", prefix->c_str(), suffix[kind], step);
     FILE *fp = fopen(name, "wb");
     if (!fp) return -1;
-    size_t w = fwrite(d, sizeof(float), n, fp);
-    fclose(fp);
-    return w == n ? 0 : -1;
+    const size_t n = (size_t)n0 * n1 * n2;
+    const size_t w = fwrite(data, sizeof(float), n, fp);
+    return (fclose(fp) == 0 && w == n) ? 0 : -1;
 }
 
-int snap_to_files(void *user, int step, int kind, const float *data, int n0, int n1, int n2)
-{   // names of 3dPureqPModeling_single_shot.cu:342-345
-    const SnapFiles *s = static_cast<const SnapFiles *>(user);
-    static const char *suffix[4] = {"", "_xz", "_yz", "_xy"};
-    char name[1024];
-    snprintf(name, sizeof(name), "%s%s%d.dat", s->prefix, suffix[kind], step);
-    return write_raw(name, data, (size_t)n0 * n1 * n2);
-}
+}  // namespace qp3d
+
+namespace {
 
 qp3d_ctx *g_ctx = nullptr;
 
@@ -232,12 +233,12 @@ void modeling3d(int nx, int ny, int nz, int nt, int ntsnap, float dx, float dy, 
     m.vp = vp; m.epsilon = epsilon; m.delta = delta; m.source = source; m.wavelet = wavelet;
     m.dlr = dlr; m.ddlr = ddlr; m.dtb = dtb; m.ddtb = ddtb; m.dfb = dfb; m.ddfb = ddfb;
     m.c = c; m.c2 = c2;
-    SnapFiles sf{snap_file ? snap_file : ""};
+    std::string prefix(snap_file ? snap_file : "");
     qp3d_snap snap;
     snap.ntsnap = ntsnap;
     snap.kinds = 0xFu;
-    snap.fn = snap_to_files;
-    snap.user = &sf;
+    snap.fn = qp3d::write_snapshot_files;
+    snap.user = &prefix;
     rc = qp3d_forward(g_ctx, &g, &m, record, (snapflag == 1 && ntsnap > 0) ? &snap : nullptr);
     if (rc)
         fprintf(stderr, "modeling3d: %s: %s\n", qp3d_strerror(rc), qp3d_ctx_last_error(g_ctx));

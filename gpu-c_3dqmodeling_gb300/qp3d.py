@@ -43,7 +43,36 @@ class Snap(ctypes.Structure):
                 ("user", ctypes.c_void_p)]
 
 
-# every symbol include/qp3d.h declares
+PATH_MAX = 256
+
+
+class Parameters(ctypes.Structure):
+    _fields_ = ([("dt", ctypes.c_float), ("nt", ctypes.c_int), ("ntsnap", ctypes.c_int),
+                 ("Nx0", ctypes.c_int), ("Ny0", ctypes.c_int), ("Nz0", ctypes.c_int),
+                 ("dx", ctypes.c_float), ("dy", ctypes.c_float), ("dz", ctypes.c_float),
+                 ("fm", ctypes.c_float), ("amp", ctypes.c_float), ("alpha", ctypes.c_float),
+                 ("sx0", ctypes.c_int), ("sy0", ctypes.c_int), ("sz0", ctypes.c_int),
+                 ("gx0", ctypes.c_int), ("gy0", ctypes.c_int), ("gz0", ctypes.c_int),
+                 ("nxshot", ctypes.c_int), ("nyshot", ctypes.c_int), ("dxshot", ctypes.c_int),
+                 ("dyshot", ctypes.c_int), ("hx", ctypes.c_int), ("hy", ctypes.c_int),
+                 ("pml", ctypes.c_int)] +
+                [(n, ctypes.c_char * PATH_MAX) for n in (
+                    "vp_file", "eps_file", "del_file", "recfull_file", "recdir_file",
+                    "recmut_file", "recxz_file", "recyz_file", "snap_direct", "snap_full")] +
+                [("multishot", ctypes.c_int), ("muteflag", ctypes.c_int),
+                 ("snapflag_full", ctypes.c_int), ("snapflag_direct", ctypes.c_int)])
+
+
+DIRECT_SOURCE_CELL, DIRECT_ZERO, DIRECT_VALUES = 0, 1, 2
+
+
+class RunOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("direct_model", ctypes.c_int),
+                ("direct_vp", ctypes.c_float), ("direct_eps", ctypes.c_float),
+                ("direct_del", ctypes.c_float), ("verbose", ctypes.c_int)]
+
+
+# every symbol include/qp3d.h and include/qp3d_driver.h declare
 EXPORTS = [
     "qp3d_version", "qp3d_strerror", "qp3d_ctx_create", "qp3d_ctx_destroy",
     "qp3d_ctx_last_error", "qp3d_forward", "qp3d_shot_load", "qp3d_shot_reset",
@@ -54,6 +83,7 @@ EXPORTS = [
     "qp3d_event_elapsed",
     "qp3d_host_alloc", "qp3d_host_free", "qp3d_gradmax_noalloc", "qp3d_fdcoff1", "qp3d_fdcoff2", "qp3d_pmlcoff",
     "qp3d_source", "qp3d_extend_model", "qp3d_absmax", "qp3d_readmodel3d",
+    "qp3d_parse_parameter_file", "qp3d_run_parameter_file",
 ]
 
 _lib = None
@@ -110,6 +140,10 @@ def load():
         "qp3d_extend_model": (None, [_vp, _vp] + [ctypes.c_int] * 4),
         "qp3d_absmax": (ctypes.c_float, [_vp, ctypes.c_size_t]),
         "qp3d_readmodel3d": (ctypes.c_int, [ctypes.c_char_p, _vp] + [ctypes.c_int] * 9),
+        "qp3d_parse_parameter_file": (ctypes.c_int, [ctypes.c_char_p, P(Parameters),
+                                                     ctypes.c_char_p, ctypes.c_size_t]),
+        "qp3d_run_parameter_file": (ctypes.c_int, [ctypes.c_char_p, P(RunOptions),
+                                                   ctypes.c_char_p, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -166,6 +200,23 @@ def extend_model(interior, nx, ny, nz, pml):
 def absmax(a):
     a = np.ascontiguousarray(a, np.float32).ravel()
     return float(load().qp3d_absmax(_p(a), a.size))
+
+
+def parse_parameter_file(path):
+    """qp3d_parse_parameter_file -> (rc, Parameters, message)."""
+    prm = Parameters()
+    err = ctypes.create_string_buffer(512)
+    rc = load().qp3d_parse_parameter_file(str(path).encode(), ctypes.byref(prm), err, len(err))
+    return rc, prm, err.value.decode()
+
+
+def run_parameter_file(path, device=0, direct_model=DIRECT_SOURCE_CELL, direct=(0.0, 0.0, 0.0),
+                       verbose=False):
+    """qp3d_run_parameter_file -> (rc, message)."""
+    o = RunOptions(device, direct_model, direct[0], direct[1], direct[2], int(verbose))
+    err = ctypes.create_string_buffer(512)
+    rc = load().qp3d_run_parameter_file(str(path).encode(), ctypes.byref(o), err, len(err))
+    return rc, err.value.decode()
 
 
 def pml_state_size(nx, ny, nz, pml):
