@@ -19,7 +19,9 @@ def _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=None, sz=None, amp=
     vp = qp3d.extend_model(vp_i, nx, ny, nz, pml)
     eps = qp3d.extend_model(eps_i, nx, ny, nz, pml)
     dl = qp3d.extend_model(del_i, nx, ny, nz, pml)
-    vpmax = np.float32((1 + 2 * qp3d.absmax(eps)) * qp3d.absmax(vp))
+    # float arithmetic throughout, as 3dPureqPModeling.c:227 computes vpmax
+    vpmax = (np.float32(1) + np.float32(2) * np.float32(qp3d.absmax(eps))) * \
+        np.float32(qp3d.absmax(vp))
     prof = qp3d.pmlcoff(pml, float(vpmax), dx, dx, dx)
     if src_xyz is None:   # 3dPureqPModeling1.0.c:263-265
         src_xyz = ((hx - 1) // 2, (hy - 1) // 2, 0)

@@ -85,8 +85,10 @@ def _finish(O, c, vols):
     hx, hy, Nz0, pml = c["hx"], c["hy"], c["Nz0"], c["pml"]
     nx, ny, nz = hx + 2 * pml, hy + 2 * pml, Nz0 + 2 * pml
     vp, eps, de = vols
-    vpmax = np.float32((1 + 2 * O.lib().oracle_absmax(O._ptr(eps), eps.size)) *
-                       O.lib().oracle_absmax(O._ptr(vp), vp.size))
+    # float arithmetic throughout, as 3dPureqPModeling1.0.c computes vpmax
+    e = np.float32(O.lib().oracle_absmax(O._ptr(eps), eps.size))
+    v = np.float32(O.lib().oracle_absmax(O._ptr(vp), vp.size))
+    vpmax = (np.float32(1) + np.float32(2) * e) * v
     prof = O.pmlcoff(pml, float(vpmax), c["dx"], c["dx"], c["dx"])
     sx1, sy1, sz1 = (hx - 1) // 2 + pml, (hy - 1) // 2 + pml, pml
     src, wav = O.source(sx1, sy1, sz1, c["fm"], c["amp"], c["alpha"], c["dt"], c["dx"], c["dx"],

@@ -51,8 +51,9 @@ def make_inputs(hx, hy, nz0, pml, nt, src, sz_i, seed, fm, alpha):
         rl.ref_extend_model(O._ptr(inp), O._ptr(out), nx, ny, nz, pml)
         vols.append(out)
     vp, eps, dl = vols
-    vpmax = np.float32((1 + 2 * rl.ref_absmax(O._ptr(eps), nx, ny, nz)) *
-                       rl.ref_absmax(O._ptr(vp), nx, ny, nz))
+    # float arithmetic throughout, as 3dPureqPModeling.c:227 computes vpmax
+    vpmax = (np.float32(1) + np.float32(2) * np.float32(rl.ref_absmax(O._ptr(eps), nx, ny, nz))) \
+        * np.float32(rl.ref_absmax(O._ptr(vp), nx, ny, nz))
     prof = [np.zeros(pml, np.float32) for _ in range(6)]
     dx = 10.0
     dt = 5e-4
