@@ -8,8 +8,7 @@
 // resident, the maximum is a device reduction, the receiver plane is written
 // by the step kernel, and nothing crosses the host link inside the time loop
 // except optional snapshots.
-#include "qp3d_internal.h"
-#include "qp3d.h"
+#include "qp3d_ctx.h"
 
 #include <algorithm>
 #include <cstdarg>
@@ -17,98 +16,7 @@
 #include <cstring>
 #include <vector>
 
-namespace qp3d {
-// qp3d_host.cpp: host derivations shared with the drop-in driver.
-void derive_coefs(const float *c, const float *c2, float dx, float dy, float dz, Coefs *k);
-void derive_layers(const float *d, const float *dd, int pml, float dt, float4 *out);
-}  // namespace qp3d
-
 using namespace qp3d;
-
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-struct qp3d_ctx {
-    int device = 0;
-    int nsm = 0;
-    cudaStream_t stream = nullptr;
-    EncodeTiledFn encode = nullptr;
-    char err[512] = {0};
-
-    // shot
-    bool loaded = false;
-    qp3d_geom g{};
-    int ldy = 0;
-    long long plane = 0, vol = 0;
-    int hx = 0, hy = 0;
-    int tile_x = 0, nxt = 0, nyt = 0, nchunks = 0, chunk_z = 0;
-    size_t smem = 0;
-    bool rec_fused = true;
-    float *U[3] = {nullptr, nullptr, nullptr};
-    float *K = nullptr, *E2 = nullptr, *R8 = nullptr;
-    float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21[2] = {};
-    float *record = nullptr;
-    float *gmax = nullptr;
-    // speculative threshold: per-step window, re-run flags, alternatives
-    float *win = nullptr;
-    int *redo = nullptr;
-    unsigned *alt_count = nullptr;
-    float *spec_err = nullptr;
-    AltEntry *alt = nullptr;
-    unsigned alt_cap = 0;
-    float4 *layers = nullptr;
-    SrcEntry *src_fused = nullptr, *src_band = nullptr, *src_all = nullptr;
-    int n_fused = 0, n_band = 0, n_all = 0;
-    bool fuse_sources = true;
-    unsigned *errword = nullptr;
-    CUtensorMap tm[3];
-    Coefs coefs{};
-    std::vector<float> wavelet;
-    int step = 0;
-    int cur = 0;           // U[cur] holds u(step)
-    int prev = 1;          // U[prev] holds u(step-1); the third buffer receives u(step+1)
-    // snapshot staging
-    float *snap_dev = nullptr;
-    float *snap_host = nullptr;
-    size_t snap_cap = 0;
-    cudaEvent_t ev[4] = {};
-    cudaEvent_t uev[8] = {};
-    // tuning
-    int step_variant = 0, gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
-    int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
-    float delta_min = 0.02f;         // smallest half-width of the predicted window
-    unsigned tune_alt_cap = 0;
-    long long launches = 0;          // kernels launched by this context
-};
-
-// ---------------------------------------------------------------------------
-static int fail(qp3d_ctx *c, int code, const char *fmt, ...)
-{
-    if (c) {
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(c->err, sizeof(c->err), fmt, ap);
-        va_end(ap);
-    }
-    return code;
-}
-
-#define CK(call)                                                                           \
-    do {                                                                                   \
-        cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess)                                                             \
-            return fail(ctx, e_ == cudaErrorMemoryAllocation ? QP3D_ERR_NOMEM : QP3D_ERR_CUDA, \
-                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-    } while (0)
-
-// launch a library kernel: check it and count it
-#define CKL(call)                                                                          \
-    do {                                                                                   \
-        CK(call);                                                                          \
-        ++ctx->launches;                                                                   \
-    } while (0)
 
 extern "C" int qp3d_version(void) { return 10000; }
 
@@ -201,6 +109,8 @@ extern "C" void qp3d_ctx_destroy(qp3d_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_shot(ctx);
+    batch_free(ctx->batch);
+    ctx->batch = nullptr;
     if (ctx->errword) cudaFree(ctx->errword);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -213,19 +123,19 @@ extern "C" void qp3d_ctx_destroy(qp3d_ctx *ctx)
 // ---------------------------------------------------------------------------
 static int check_geom(qp3d_ctx *ctx, const qp3d_geom *g)
 {
-    if (!g) return fail(ctx, QP3D_ERR_ARG, "null geometry");
+    if (!g) return ctx_fail(ctx, QP3D_ERR_ARG, "null geometry");
     if (g->nx < 11 || g->ny < 11 || g->nz < 11)
-        return fail(ctx, QP3D_ERR_ARG, "grid %dx%dx%d smaller than 11 cells", g->nx, g->ny, g->nz);
+        return ctx_fail(ctx, QP3D_ERR_ARG, "grid %dx%dx%d smaller than 11 cells", g->nx, g->ny, g->nz);
     if (g->pml < 0 || g->pml > kMaxPml || 2 * g->pml >= g->nx || 2 * g->pml >= g->ny ||
         2 * g->pml >= g->nz)
-        return fail(ctx, QP3D_ERR_ARG, "pml %d invalid for grid %dx%dx%d", g->pml, g->nx, g->ny,
+        return ctx_fail(ctx, QP3D_ERR_ARG, "pml %d invalid for grid %dx%dx%d", g->pml, g->nx, g->ny,
                     g->nz);
-    if (g->nt < 0) return fail(ctx, QP3D_ERR_ARG, "nt < 0");
-    if (g->sz < 0 || g->sz >= g->nz) return fail(ctx, QP3D_ERR_ARG, "sz %d outside [0,%d)", g->sz, g->nz);
+    if (g->nt < 0) return ctx_fail(ctx, QP3D_ERR_ARG, "nt < 0");
+    if (g->sz < 0 || g->sz >= g->nz) return ctx_fail(ctx, QP3D_ERR_ARG, "sz %d outside [0,%d)", g->sz, g->nz);
     if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->dt > 0))
-        return fail(ctx, QP3D_ERR_ARG, "non-positive spacing or time step");
+        return ctx_fail(ctx, QP3D_ERR_ARG, "non-positive spacing or time step");
     long long n = (long long)g->nx * g->ny * g->nz;
-    if (n > (1ll << 40)) return fail(ctx, QP3D_ERR_ARG, "grid too large");
+    if (n > (1ll << 40)) return ctx_fail(ctx, QP3D_ERR_ARG, "grid too large");
     return QP3D_OK;
 }
 
@@ -240,7 +150,7 @@ static int make_tmap(qp3d_ctx *ctx, float *base, CUtensorMap *tm)
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(ctx, QP3D_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    if (r != CUDA_SUCCESS) return ctx_fail(ctx, QP3D_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return QP3D_OK;
 }
 
@@ -294,9 +204,9 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     int rc = check_geom(ctx, g);
     if (rc) return rc;
     if (!m || !m->vp || !m->epsilon || !m->delta || !m->wavelet || !m->c || !m->c2)
-        return fail(ctx, QP3D_ERR_ARG, "missing model input");
+        return ctx_fail(ctx, QP3D_ERR_ARG, "missing model input");
     if (g->pml > 0 && (!m->dlr || !m->ddlr || !m->dtb || !m->ddtb || !m->dfb || !m->ddfb))
-        return fail(ctx, QP3D_ERR_ARG, "missing PML profiles");
+        return ctx_fail(ctx, QP3D_ERR_ARG, "missing PML profiles");
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
 
@@ -401,7 +311,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
 extern "C" int qp3d_shot_reset(qp3d_ctx *ctx)
 {
     if (!ctx) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
     CK(cudaSetDevice(ctx->device));
     size_t vb = (size_t)ctx->vol * sizeof(float);
     float *zero[] = {ctx->U[0],  ctx->U[1],  ctx->U[2],  ctx->W1[0], ctx->W1[1], ctx->W1[2],
@@ -528,9 +438,9 @@ extern "C" int qp3d_shot_launches_per_step(const qp3d_ctx *ctx)
 extern "C" int qp3d_shot_advance(qp3d_ctx *ctx, int nsteps)
 {
     if (!ctx || nsteps < 0) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
     if (ctx->step + nsteps > ctx->g.nt)
-        return fail(ctx, QP3D_ERR_ARG, "advance past nt (%d + %d > %d)", ctx->step, nsteps, ctx->g.nt);
+        return ctx_fail(ctx, QP3D_ERR_ARG, "advance past nt (%d + %d > %d)", ctx->step, nsteps, ctx->g.nt);
     CK(cudaSetDevice(ctx->device));
     for (int i = 0; i < nsteps; ++i) {
         int rc = enqueue_step(ctx, nullptr, nullptr, nullptr, nullptr);
@@ -547,7 +457,7 @@ extern "C" int qp3d_shot_sync(qp3d_ctx *ctx)
     if (ctx->errword) {
         unsigned e = 0;
         CK(cudaMemcpy(&e, ctx->errword, sizeof(e), cudaMemcpyDeviceToHost));
-        if (e) return fail(ctx, QP3D_ERR_TIMEOUT, "device wait timed out (flags 0x%x)", e);
+        if (e) return ctx_fail(ctx, QP3D_ERR_TIMEOUT, "device wait timed out (flags 0x%x)", e);
     }
     return QP3D_OK;
 }
@@ -557,8 +467,8 @@ extern "C" int qp3d_shot_step(const qp3d_ctx *ctx) { return ctx ? ctx->step : -1
 extern "C" int qp3d_shot_read_record(qp3d_ctx *ctx, int k0, int nsteps, float *out)
 {
     if (!ctx || !out || k0 < 0 || nsteps < 0) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
-    if (k0 + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "record range past nt");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (k0 + nsteps > ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "record range past nt");
     int rc = qp3d_shot_sync(ctx);
     if (rc) return rc;
     size_t row = (size_t)ctx->hx * ctx->hy;
@@ -570,8 +480,8 @@ extern "C" int qp3d_shot_read_record(qp3d_ctx *ctx, int k0, int nsteps, float *o
 extern "C" int qp3d_shot_read_uxyzmax(qp3d_ctx *ctx, int k0, int nsteps, float *out)
 {
     if (!ctx || !out || k0 < 0 || nsteps < 0) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
-    if (k0 + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "range past nt");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (k0 + nsteps > ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "range past nt");
     int rc = qp3d_shot_sync(ctx);
     if (rc) return rc;
     CK(cudaMemcpy(out, ctx->gmax + k0, nsteps * sizeof(float), cudaMemcpyDeviceToHost));
@@ -646,8 +556,8 @@ extern "C" int qp3d_shot_write_state(qp3d_ctx *ctx, int step, const float *u_pre
                                      const float *u_cur, const float *pml_state)
 {
     if (!ctx) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
-    if (step < 0 || step > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "step out of range");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (step < 0 || step > ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "step out of range");
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->step = step;
@@ -681,7 +591,7 @@ extern "C" int qp3d_shot_write_state(qp3d_ctx *ctx, int step, const float *u_pre
 extern "C" int qp3d_shot_read_state(qp3d_ctx *ctx, float *u_prev, float *u_cur, float *pml_state)
 {
     if (!ctx) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
     int rc = qp3d_shot_sync(ctx);
     if (rc) return rc;
     if (u_prev && (rc = download_vol(ctx, u_prev, ctx->U[ctx->prev]))) return rc;
@@ -737,7 +647,7 @@ static int ensure_snap(qp3d_ctx *ctx, size_t n)
 extern "C" int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap)
 {
     if (!ctx || !snap || !snap->fn) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
     const qp3d_geom &g = ctx->g;
     const int pml = g.pml, hx = ctx->hx, hy = ctx->hy, hz = g.nz - 2 * pml;
     const float *u = ctx->U[ctx->cur];
@@ -761,7 +671,7 @@ extern "C" int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap)
         rc = qp3d_shot_sync(ctx);
         if (rc) return rc;
         if (snap->fn(snap->user, k, r.kind, ctx->snap_host, r.n0, r.n1, r.n2) != 0)
-            return fail(ctx, QP3D_ERR_CALLBACK, "snapshot callback failed at step %d", k);
+            return ctx_fail(ctx, QP3D_ERR_CALLBACK, "snapshot callback failed at step %d", k);
     }
     return QP3D_OK;
 }
@@ -795,8 +705,8 @@ extern "C" int qp3d_shot_time(qp3d_ctx *ctx, int nsteps, float *ms_total, float 
                               float *ms_gradmax)
 {
     if (!ctx || nsteps < 0) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
-    if (ctx->step + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "advance past nt");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (ctx->step + nsteps > ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "advance past nt");
     CK(cudaSetDevice(ctx->device));
     const bool per_kernel = ms_step || ms_gradmax;
     std::vector<cudaEvent_t> evs;
@@ -872,6 +782,11 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "threshold_mode") && (value == 0 || value == 1)) ctx->threshold_mode = value;
     else if (!strcmp(key, "spec_delta_ppm") && value >= 0 && value <= 250000)
         ctx->delta_min = value * 1e-6f;
+    else if (!strcmp(key, "batch_graph") && (value == 0 || value == 1)) ctx->batch_graph = value;
+    else if (!strcmp(key, "batch_tune") && (value == 0 || value == 1)) ctx->batch_tune = value;
+    else if (!strcmp(key, "batch_candidate") && value >= -1 && value < 16)
+        ctx->batch_candidate = value;
+    else if (!strcmp(key, "batch_mem_mb") && value >= 0) ctx->batch_mem_mb = value;
     else if (!strcmp(key, "alt_cap") && value >= 0) {
         ctx->tune_alt_cap = (unsigned)value;
         if (ctx->loaded) {
@@ -884,7 +799,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
             CK(cudaMalloc(&ctx->alt, (size_t)std::max(ctx->alt_cap, 1u) * sizeof(AltEntry)));
         }
     }
-    else return fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
+    else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
     if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
         CK(cudaSetDevice(ctx->device));
         CK(cudaStreamSynchronize(ctx->stream));
@@ -906,14 +821,18 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "threshold_mode")) return ctx->threshold_mode;
     if (!strcmp(key, "spec_delta_ppm")) return (int)(ctx->delta_min * 1e6f + 0.5f);
     if (!strcmp(key, "alt_cap")) return (int)ctx->alt_cap;
+    if (!strcmp(key, "batch_graph")) return ctx->batch_graph;
+    if (!strcmp(key, "batch_tune")) return ctx->batch_tune;
+    if (!strcmp(key, "batch_candidate")) return ctx->batch_candidate;
+    if (!strcmp(key, "batch_mem_mb")) return (int)ctx->batch_mem_mb;
     return QP3D_ERR_ARG;
 }
 
 extern "C" int qp3d_shot_read_stats(qp3d_ctx *ctx, int k0, int nsteps, int *redo, unsigned *alt)
 {
     if (!ctx || k0 < 0 || nsteps < 0) return QP3D_ERR_ARG;
-    if (!ctx->loaded) return fail(ctx, QP3D_ERR_STATE, "no shot loaded");
-    if (k0 + nsteps > ctx->g.nt) return fail(ctx, QP3D_ERR_ARG, "range past nt");
+    if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
+    if (k0 + nsteps > ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "range past nt");
     int rc = qp3d_shot_sync(ctx);
     if (rc) return rc;
     if (redo) CK(cudaMemcpy(redo, ctx->redo + k0, nsteps * sizeof(int), cudaMemcpyDeviceToHost));

@@ -1,0 +1,107 @@
+// qp3d_ctx.h -- the library context (internal to libqp3d).
+#pragma once
+
+#include "qp3d_internal.h"
+#include "qp3d.h"
+
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+namespace qp3d {
+// qp3d_host.cpp: host derivations shared with the drop-in driver.
+void derive_coefs(const float *c, const float *c2, float dx, float dy, float dz, Coefs *k);
+void derive_layers(const float *d, const float *dd, int pml, float dt, float4 *out);
+struct BatchState;                 // qp3d_batch.cu
+void batch_free(BatchState *b);
+}  // namespace qp3d
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+struct qp3d_ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    EncodeTiledFn encode = nullptr;
+    char err[512] = {0};
+
+    // shot
+    bool loaded = false;
+    qp3d_geom g{};
+    int ldy = 0;
+    long long plane = 0, vol = 0;
+    int hx = 0, hy = 0;
+    int tile_x = 0, nxt = 0, nyt = 0, nchunks = 0, chunk_z = 0;
+    size_t smem = 0;
+    bool rec_fused = true;
+    float *U[3] = {nullptr, nullptr, nullptr};
+    float *K = nullptr, *E2 = nullptr, *R8 = nullptr;
+    float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21[2] = {};
+    float *record = nullptr;
+    float *gmax = nullptr;
+    // speculative threshold: per-step window, re-run flags, alternatives
+    float *win = nullptr;
+    int *redo = nullptr;
+    unsigned *alt_count = nullptr;
+    float *spec_err = nullptr;
+    qp3d::AltEntry *alt = nullptr;
+    unsigned alt_cap = 0;
+    float4 *layers = nullptr;
+    qp3d::SrcEntry *src_fused = nullptr, *src_band = nullptr, *src_all = nullptr;
+    int n_fused = 0, n_band = 0, n_all = 0;
+    bool fuse_sources = true;
+    unsigned *errword = nullptr;
+    CUtensorMap tm[3];
+    qp3d::Coefs coefs{};
+    std::vector<float> wavelet;
+    int step = 0;
+    int cur = 0;           // U[cur] holds u(step)
+    int prev = 1;          // U[prev] holds u(step-1); the third buffer receives u(step+1)
+    // snapshot staging
+    float *snap_dev = nullptr;
+    float *snap_host = nullptr;
+    size_t snap_cap = 0;
+    cudaEvent_t ev[4] = {};
+    cudaEvent_t uev[8] = {};
+    // tuning
+    int step_variant = 0, gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
+    int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
+    float delta_min = 0.02f;         // smallest half-width of the predicted window
+    unsigned tune_alt_cap = 0;
+    long long launches = 0;          // kernels launched by this context
+    // batched shots (qp3d_batch)
+    qp3d::BatchState *batch = nullptr;
+    int batch_graph = 1;             // replay speculative steps from a captured graph
+    int batch_tune = 1;              // choose the tile / z-block shape by timing
+    int batch_candidate = -1;        // fixed shape (when not tuning), -1: default
+    long long batch_mem_mb = 0;      // device memory for one group of shots, 0: auto
+};
+inline int ctx_fail(qp3d_ctx *c, int code, const char *fmt, ...)
+{
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c->err, sizeof(c->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define CK(call)                                                                           \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return ctx_fail(ctx, e_ == cudaErrorMemoryAllocation ? QP3D_ERR_NOMEM : QP3D_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+// launch a library kernel: check it and count it
+#define CKL(call)                                                                          \
+    do {                                                                                   \
+        CK(call);                                                                          \
+        ++ctx->launches;                                                                   \
+    } while (0)
+

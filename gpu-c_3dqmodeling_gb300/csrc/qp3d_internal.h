@@ -2,14 +2,13 @@
 //
 // Device layout of one shot (all float32, row pitch ldy = ny rounded up to 32
 // so every row starts on a 128-byte boundary):
-//   U[2]            wavefields; U[cur] is u(k) ("u2"), U[cur^1] holds u(k-1)
-//                   on entry to a step and u(k+1) on exit (updated in place)
+//   U[3]            wavefields u(k-1), u(k), u(k+1), rotated by index: a step
+//                   never overwrites its inputs
 //   K, E2, R8       per-cell parameters (vp*dt)^2, 2*eps, 8*(eps-delta)
-//   W1[3],W3[3],P[3] PML split fields, three time levels each, rotated by
-//                   index (no copies); W21 is updated in place.  These are
-//                   full "shadow" volumes: only PML cells are ever touched,
-//                   so a cell's state lives at the cell's own index whatever
-//                   face owns it.
+//   W1[3],W3[3],P[3] PML split fields, three time levels each, and W21[2],
+//                   rotated by index (no copies).  These are full "shadow"
+//                   volumes: only PML cells are ever touched, so a cell's
+//                   state lives at the cell's own index whatever face owns it.
 //   record          nt * hx * hy receiver samples
 //   gmax            nt floats: max|grad u| of each step (bits, atomicMax)
 #pragma once
@@ -95,6 +94,50 @@ struct PlaneParams {
     AltEntry *alt;            // alternatives of this step
     unsigned *alt_count;      // &alt_count[step]
     unsigned alt_cap;
+    // batched launches only
+    int ucur;                 // index of u(k) among the shot's three buffers
+    int active;               // 0 once the shot has run all its steps
+};
+
+// One shot of a batched run, as the host lays it out in device memory; the
+// per-step PlaneParams are derived from it on the device
+// (qp3d_batch_prepare_kernel), so a captured step can be replayed.
+struct BatchShot {
+    int nx, ny, nz, ldy, pml, sz, nt, hx, hy;
+    long long plane;
+    float dt, delta_min;
+    float *U[3];
+    const float *K, *E2, *R8;
+    float *W1[3], *W3[3], *P[3], *W21[2];
+    const float4 *layers;
+    float *gmax;
+    float *record;
+    const SrcEntry *src;
+    int nsrc;
+    const float *wavelet;     // nt samples
+    float *win;               // 3 * nt
+    int *redo;                // nt
+    unsigned *alt_count;      // nt
+    float *spec_err;
+    AltEntry *alt;
+    unsigned alt_cap;
+    unsigned *err;
+};
+
+// A unit of work of a batched launch: one tile column of one shot.
+struct WorkItem {
+    int shot, tile_x, y0, x0, z0, z1;
+};
+
+// Kernel arguments of the batched plane kernels.  The coefficient tables are
+// shared by all shots of a batch (same spacing and FD tables).
+struct BatchArgs {
+    Coefs k;
+    const PlaneParams *pp;    // per shot, the current step
+    const CUtensorMap *tm;    // per shot three maps (one per u buffer)
+    const WorkItem *work;
+    int nwork;
+    int *queue;               // next work item (zeroed by the prepare kernel)
 };
 
 struct Shot;   // host-side, defined in qp3d_api.cu
@@ -124,6 +167,18 @@ cudaError_t launch_params(const float *vp, const float *eps, const float *del,
                           float *K, float *E2, float *R8, long long n, float dt,
                           cudaStream_t stream);
 size_t plane_smem_bytes(int tile_x, int pml);
+
+// Batched launches (persistent CTAs pulling work items).  kind: 0 gradmax,
+// 1 exact step (gated per shot), 2 speculative step.
+size_t batch_smem_bytes(int tile_x, int pml);
+cudaError_t launch_batch_prepare(const BatchShot *shots, int nshots, PlaneParams *pp, int *ctr,
+                                 int *queues, int spec, cudaStream_t stream);
+cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threads, size_t smem,
+                               cudaStream_t stream);
+cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,
+                               cudaStream_t stream);
+int batch_plane_threads(int tile_x);
+cudaError_t batch_ctas_per_sm(int kind, int threads, size_t smem, int *n);
 cudaError_t configure_gradmax_partial();
 cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid,
                                    size_t smem, cudaStream_t stream, float *partial,

@@ -340,6 +340,9 @@ __device__ void pipe_init(const Pipe &P)
         mbar_init(&P.empty[s], P.ncw);
     }
     fence_barrier_init();
+    // a CTA that takes another tile reuses shared memory its threads read
+    // and wrote (generic proxy) as TMA destination (async proxy)
+    fence_proxy_async();
 }
 
 // Refills, done by thread 0 of the CTA (which also computes).  Before
@@ -372,20 +375,36 @@ __device__ void pipe_drain(const Pipe &P, int next_issue)
     for (int j = max(0, next_issue - kRing); j < next_issue; ++j) (void)pipe_wait(P, j);
 }
 
-__device__ __forceinline__ void pipe_setup(Pipe &P, unsigned char *smem, const PlaneParams &p,
+__device__ __forceinline__ void pipe_setup(Pipe &P, unsigned char *smem, int tile_x, int pml,
                                            int y0, int x0, int z0, int nzc)
 {
-    const SmemLayout L = smem_layout(p.tile_x, p.pml);
+    const SmemLayout L = smem_layout(tile_x, pml);
     P.ring = reinterpret_cast<float *>(smem);
     P.full = reinterpret_cast<uint64_t *>(smem + L.bar_off);
     P.empty = P.full + kRing;
     P.slot_floats = L.slot_floats;
-    P.box_bytes = (unsigned)((p.tile_x + 2 * kRadius) * kBoxY * 4);
+    P.box_bytes = (unsigned)((tile_x + 2 * kRadius) * kBoxY * 4);
     P.nplanes = nzc + 2 * kRadius;
     P.zfirst = z0 - kRadius;
     P.c0 = y0 - kHaloY;
     P.c1 = x0 - kRadius;
-    P.ncw = (kQuadsY * p.tile_x + 31) / 32;
+    P.ncw = blockDim.x >> 5;   // every warp of the CTA releases every slot
+}
+
+__device__ __forceinline__ void pipe_setup(Pipe &P, unsigned char *smem, const PlaneParams &p,
+                                           int y0, int x0, int z0, int nzc)
+{
+    pipe_setup(P, smem, p.tile_x, p.pml, y0, x0, z0, nzc);
+}
+
+// Before a CTA reuses its barriers for another tile (thread 0, after a CTA
+// barrier; every load of the previous tile has been waited for).
+__device__ void pipe_inval(const Pipe &P)
+{
+    for (int s = 0; s < kRing; ++s) {
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&P.full[s])) : "memory");
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&P.empty[s])) : "memory");
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -518,6 +537,71 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if ((tid & 31) == 0 && mx > 0.0f)
         atomicMax(reinterpret_cast<unsigned *>(p.gmax + p.step), __float_as_uint(mx));
+}
+
+// ---------------------------------------------------------------------------
+// gradmax of one tile column [z0, z1) for the batched launches: the
+// arithmetic of qp3d_gradmax_kernel<false>.  With REUSE the CTA's barriers
+// are invalidated at the end so that it can take another tile; the return
+// value (false: a wait timed out) is then the same in every thread.
+// ---------------------------------------------------------------------------
+template <bool REUSE>
+__device__ __forceinline__ bool gradmax_tile(const CUtensorMap *tm, const PlaneParams &p,
+                                             const Coefs &k, int tile_x, int y0, int x0, int z0,
+                                             int z1, unsigned char *smem)
+{
+    const int tid = threadIdx.x;
+    const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
+    const int nzc = z1 - z0;
+    Pipe P;
+    pipe_setup(P, smem, tile_x, p.pml, y0, x0, z0, nzc);
+    int next_issue = 0;
+    if (tid == 0) {
+        pipe_init(P);
+        next_issue = min(kRing, P.nplanes);
+        for (int i = 0; i < next_issue; ++i) pipe_issue(P, tm, i);
+    }
+    __syncthreads();
+    const int x = x0 + r, yq = y0 + 4 * q;
+    const bool row_ok = (r < tile_x) && (x < p.nx - kRadius);
+    bool cell_ok[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < p.ny - kRadius);
+    const int rc = (r + kRadius) * kBoxY + kHaloY + 4 * q;
+    float mx = 0.0f;
+    bool ok = true;
+    int waited = 0;
+    for (int t = 0; t < nzc; ++t) {
+        if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, tm, t, next_issue)) ok = false;
+        while (ok && waited <= t + 2 * kRadius) {
+            ok = pipe_wait(P, waited);
+            if (ok) ++waited;
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
+        if (row_ok) {
+            float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+            quad_derivs<false>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (cell_ok[j])
+                    mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+        }
+        pipe_release(P, t);
+    }
+    if (!ok) {
+        atomicOr(p.err, kErrWaitTimeout);
+        if (tid == 0) pipe_drain(P, next_issue);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((tid & 31) == 0 && mx > 0.0f)
+        atomicMax(reinterpret_cast<unsigned *>(p.gmax + p.step), __float_as_uint(mx));
+    if (REUSE) {
+        ok = __syncthreads_and(ok) != 0;
+        if (tid == 0 && ok) pipe_inval(P);
+    }
+    return ok;
 }
 
 // ---------------------------------------------------------------------------
@@ -701,13 +785,15 @@ __device__ __forceinline__ float aniso_s(float h2, float m2, float e2x, float r8
     return fmaf(0.5f, __fsqrt_rn(__fsub_rn(1.0f, qq)), 0.5f);
 }
 
-template <bool SPEC>
-__global__ void __launch_bounds__(kThreads, 2)
-    qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
+// One tile column [z0, z1) of the step.  The grid kernel below runs one per
+// CTA; the batched kernel runs many per CTA (REUSE: barriers invalidated at
+// the end, return value uniform over the CTA; false = a wait timed out).
+template <bool SPEC, bool REUSE>
+__device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlaneParams &p,
+                                          const Coefs &k, int tile_x, int y0, int x0, int z0,
+                                          int z1, bool win_writer, unsigned char *smem)
 {
-    if (!SPEC && p.gate && *p.gate == 0) return;
-    extern __shared__ __align__(128) unsigned char smem[];
-    const SmemLayout L = smem_layout(p.tile_x, p.pml);
+    const SmemLayout L = smem_layout(tile_x, p.pml);
     float4 *tab = reinterpret_cast<float4 *>(smem + L.tab_off);
     SrcEntry *csrc = reinterpret_cast<SrcEntry *>(smem + L.src_off);
     float *misc = reinterpret_cast<float *>(smem + L.misc_off);
@@ -715,26 +801,22 @@ __global__ void __launch_bounds__(kThreads, 2)
 
     const int tid = threadIdx.x, lane = tid & 31;
     const int q = tid & (kQuadsY - 1), r = tid / kQuadsY;
-    const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
-    const int z0 = kRadius + blockIdx.z * p.chunk_z;
-    const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
-    if (z0 >= z1) return;
     const int nzc = z1 - z0;
     Pipe P;
-    pipe_setup(P, smem, p, y0, x0, z0, nzc);
+    pipe_setup(P, smem, tile_x, p.pml, y0, x0, z0, nzc);
 
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml;
     int next_issue = 0;
     if (tid == 0) {
         pipe_init(P);
         next_issue = min(kRing, P.nplanes);
-        for (int i = 0; i < next_issue; ++i) pipe_issue(P, &tm_u, i);
+        for (int i = 0; i < next_issue; ++i) pipe_issue(P, tm, i);
         if (SPEC) {
             float lo, hi, pred;
             spec_window(p, lo, hi, pred);
             misc[0] = threshold_m2(lo);
             misc[1] = threshold_m2(hi);
-            if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) {
+            if (win_writer) {
                 p.win[0] = lo;
                 p.win[1] = hi;
                 p.win[2] = pred;
@@ -745,7 +827,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         int n = 0;
         for (int e = 0; e < p.nsrc; ++e) {
             SrcEntry s = p.src[e];
-            if (s.x >= x0 && s.x < x0 + p.tile_x && s.y >= y0 && s.y < y0 + kTileY && s.z >= z0 &&
+            if (s.x >= x0 && s.x < x0 + tile_x && s.y >= y0 && s.y < y0 + kTileY && s.z >= z0 &&
                 s.z < z1 && n < kMaxFusedSources)
                 csrc[n++] = s;
         }
@@ -757,7 +839,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int ncsrc = misc_i[0];
 
     const int x = x0 + r, yq = y0 + 4 * q;
-    const bool row_ok = (r < p.tile_x) && (x < nx - kRadius);
+    const bool row_ok = (r < tile_x) && (x < nx - kRadius);
     bool cell_ok[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < ny - kRadius);
@@ -776,7 +858,6 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     const bool xy_face = row_ok && (fx >= 0 || any_fy);
     const int hy = ny - 2 * pml;
-    const Coefs &k = p.k;
     const float dt = p.dt;
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
 
@@ -804,7 +885,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             p1 = ldg4(p.po + base);   p2 = ldg4(p.pc + base);
             w21 = ldg4(p.w21o + base);
         }
-        if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, &tm_u, t, next_issue)) ok = false;
+        if (tid == 0 && t >= kPrefetch + 1 && !pipe_refill(P, tm, t, next_issue)) ok = false;
         while (ok && waited <= t + 2 * kRadius) {
             ok = pipe_wait(P, waited);
             if (ok) ++waited;
@@ -949,6 +1030,25 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (lane == 0 && mx > 0.0f)
             atomicMax(reinterpret_cast<unsigned *>(p.gmax + p.step), __float_as_uint(mx));
     }
+    if (REUSE) {
+        ok = __syncthreads_and(ok) != 0;
+        if (tid == 0 && ok) pipe_inval(P);
+    }
+    return ok;
+}
+
+template <bool SPEC>
+__global__ void __launch_bounds__(kThreads, 2)
+    qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
+{
+    if (!SPEC && p.gate && *p.gate == 0) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int y0 = blockIdx.x * kTileY, x0 = kRadius + blockIdx.y * p.tile_x;
+    const int z0 = kRadius + blockIdx.z * p.chunk_z;
+    const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
+    if (z0 >= z1) return;
+    step_tile<SPEC, false>(&tm_u, p, p.k, p.tile_x, y0, x0, z0, z1,
+                           blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
 }
 
 // Derivatives of u at one cell from global memory, in the same operation
@@ -984,20 +1084,21 @@ __device__ void cell_derivs(const float *u, long long i, long long sx, long long
 // is recomputed with S = 1 from the step's (untouched) inputs; otherwise
 // *redo = 1 and the gated exact re-run recomputes the whole step.  Also
 // records the relative error of the prediction.
-__global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_err)
+__device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k, int *redo,
+                                           float *spec_err, unsigned block, unsigned nblocks)
 {
     const float M = p.gmax[p.step];
     const float lo = p.win[0], hi = p.win[1], pred = p.win[2];
     const unsigned n = *p.alt_count;
     const bool inside = (M >= lo) && (M <= hi) && (n <= p.alt_cap);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (block == 0 && threadIdx.x == 0) {
         *redo = inside ? 0 : 1;
         *spec_err = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
     }
     if (!inside) return;
     const float T2 = threshold_m2(M);
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml, hy = ny - 2 * pml;
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (unsigned i = block * blockDim.x + threadIdx.x; i < n; i += nblocks * blockDim.x) {
         const AltEntry e = p.alt[i];
         if (e.m2 > T2) continue;
         const long long idx = e.idx;
@@ -1011,7 +1112,7 @@ __global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_er
             continue;
         }
         float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
-        cell_derivs(p.u_cur, idx, p.ldy, p.plane, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        cell_derivs(p.u_cur, idx, p.ldy, p.plane, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
         const float K = p.prm_k[idx];
         const float KS = __fmul_rn(K, 1.0f);
         const float e2 = __fadd_rn(1.0f, p.prm_e[idx]);
@@ -1040,6 +1141,11 @@ __global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_er
         if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
             p.record[(long long)(x - pml) * hy + (y - pml)] = out;
     }
+}
+
+__global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_err)
+{
+    fixup_body(p, p.k, redo, spec_err, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1114,12 +1220,154 @@ __global__ void qp3d_params_kernel(float *K, float *E2, float *R8, long long n, 
 }
 
 // ---------------------------------------------------------------------------
+// Batched shots.  Per time step:
+//   qp3d_batch_prepare_kernel   reads the step counter k, writes every shot's
+//                               PlaneParams of step k (buffer rotation,
+//                               wavelet[k], record plane, per-step slots),
+//                               zeroes the work queues, sets the counter to
+//                               k + 1.  The step is therefore the same
+//                               sequence of launches for every k and can be
+//                               captured once in a CUDA graph.
+//   qp3d_batch_plane_kernel     persistent CTAs (as many as are resident)
+//                               take work items -- one tile column of one
+//                               shot -- from an atomic queue and run the
+//                               gradmax or step tile body on it; uneven shot
+//                               sizes mix in one launch.
+//   qp3d_batch_fixup_kernel     the speculative fix-up, blockIdx.y = shot.
+// ---------------------------------------------------------------------------
+__global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, PlaneParams *pp,
+                                          int *ctr, int *queues, int spec)
+{
+    const int k = *ctr;
+    for (int s = threadIdx.x; s < nshots; s += blockDim.x) {
+        const BatchShot &b = shots[s];
+        PlaneParams p;
+        memset(&p, 0, sizeof(p));
+        p.nx = b.nx; p.ny = b.ny; p.nz = b.nz; p.ldy = b.ldy; p.pml = b.pml; p.sz = b.sz;
+        p.plane = b.plane;
+        p.dt = b.dt;
+        p.step = k;
+        p.err = b.err;
+        p.active = k < b.nt ? 1 : 0;
+        if (p.active) {
+            // the host's rotation of qp3d_shot_advance from a reset shot
+            const int a = (3 - k % 3) % 3, bb = (a + 1) % 3, c = (a + 2) % 3;
+            p.ucur = a;
+            p.u_cur = b.U[a]; p.u_prev = b.U[bb]; p.u_out = b.U[c];
+            p.prm_k = b.K; p.prm_e = b.E2; p.prm_r = b.R8;
+            const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
+            p.w1o = b.W1[lo]; p.w1c = b.W1[lc]; p.w1n = b.W1[ln];
+            p.w3o = b.W3[lo]; p.w3c = b.W3[lc]; p.w3n = b.W3[ln];
+            p.po = b.P[lo];   p.pc = b.P[lc];   p.pn = b.P[ln];
+            p.w21o = b.W21[k % 2];
+            p.w21n = b.W21[(k + 1) % 2];
+            p.layers = b.layers;
+            p.gmax = b.gmax;
+            p.record = b.record + (long long)k * b.hx * b.hy;
+            p.src = b.src;
+            p.nsrc = b.nsrc;
+            p.wavelet = b.wavelet[k];
+            p.spec = spec;
+            p.gate = spec ? b.redo + k : nullptr;
+            p.win = b.win + 3 * (long long)k;
+            p.spec_err = b.spec_err;
+            p.delta_min = b.delta_min;
+            p.alt = b.alt;
+            p.alt_count = b.alt_count + k;
+            p.alt_cap = b.alt_cap;
+        }
+        pp[s] = p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        queues[0] = queues[1] = queues[2] = queues[3] = 0;
+        *ctr = k + 1;
+    }
+}
+
+constexpr size_t kParamBytes = (sizeof(PlaneParams) + 127) & ~(size_t)127;
+
+size_t batch_smem_bytes(int tile_x, int pml) { return kParamBytes + plane_smem_bytes(tile_x, pml); }
+
+// KIND 0: gradmax, 1: exact step (skipped for shots whose gate is 0),
+// 2: speculative step.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, 2) qp3d_batch_plane_kernel(const __grid_constant__ BatchArgs b)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    // item slot double-buffered by iteration: thread 0 can run one iteration
+    // ahead of the others only on the skip path, which has no second barrier
+    __shared__ int s_item[2], s_run[2];
+    PlaneParams *sp = reinterpret_cast<PlaneParams *>(smem);
+    unsigned char *body = smem + kParamBytes;
+    for (int iter = 0;; ++iter) {
+        const int slot = iter & 1;
+        if (threadIdx.x == 0) {
+            const int it = atomicAdd(b.queue, 1);
+            int run = 0;
+            if (it < b.nwork) {
+                const PlaneParams &g = b.pp[b.work[it].shot];
+                run = g.active != 0;
+                if (KIND == 1) run = run && !(g.gate && *g.gate == 0);
+            }
+            s_item[slot] = it;
+            s_run[slot] = run;
+        }
+        __syncthreads();
+        const int it = s_item[slot];
+        if (it >= b.nwork) return;
+        if (!s_run[slot]) continue;
+        const WorkItem w = b.work[it];
+        {
+            const unsigned *src = reinterpret_cast<const unsigned *>(b.pp + w.shot);
+            unsigned *dst = reinterpret_cast<unsigned *>(sp);
+            for (int i = threadIdx.x; i < (int)(sizeof(PlaneParams) / 4); i += blockDim.x)
+                dst[i] = src[i];
+        }
+        const CUtensorMap *tm = b.tm + 3 * w.shot;
+        if (threadIdx.x == 0)   // maps written by the host before the launch
+            for (int i = 0; i < 3; ++i)
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm + i)
+                             : "memory");
+        __syncthreads();
+        const PlaneParams &p = *sp;
+        tm += p.ucur;
+        bool ok;
+        if (KIND == 0) {
+            ok = gradmax_tile<true>(tm, p, b.k, w.tile_x, w.y0, w.x0, w.z0, w.z1, body);
+        } else {
+            const bool first = w.y0 == 0 && w.x0 == kRadius && w.z0 == kRadius;
+            ok = step_tile<KIND == 2, true>(tm, p, b.k, w.tile_x, w.y0, w.x0, w.z0, w.z1, first,
+                                            body);
+        }
+        if (!ok) return;
+    }
+}
+
+__global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
+{
+    const PlaneParams &p = b.pp[blockIdx.y];
+    if (!p.active || !p.spec) return;
+    fixup_body(p, b.k, const_cast<int *>(p.gate), const_cast<float *>(p.spec_err), blockIdx.x,
+               gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 cudaError_t configure_kernels()
 {
     const int bytes = 200 * 1024;
     cudaError_t e;
+    if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<0>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<1>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
+    if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<2>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+        return e;
     if ((e = cudaFuncSetAttribute(qp3d_step_kernel<true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
@@ -1178,6 +1426,42 @@ cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaS
                          int nsm)
 {
     qp3d_fixup_kernel<<<8 * nsm, 256, 0, stream>>>(p, redo, spec_err);
+    return cudaGetLastError();
+}
+
+int batch_plane_threads(int tile_x) { return plane_threads(tile_x); }
+
+cudaError_t launch_batch_prepare(const BatchShot *shots, int nshots, PlaneParams *pp, int *ctr,
+                                 int *queues, int spec, cudaStream_t stream)
+{
+    qp3d_batch_prepare_kernel<<<1, 128, 0, stream>>>(shots, nshots, pp, ctr, queues, spec);
+    return cudaGetLastError();
+}
+
+cudaError_t batch_ctas_per_sm(int kind, int threads, size_t smem, int *n)
+{
+    const void *f = kind == 0 ? (const void *)qp3d_batch_plane_kernel<0>
+                  : kind == 1 ? (const void *)qp3d_batch_plane_kernel<1>
+                              : (const void *)qp3d_batch_plane_kernel<2>;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, f, threads, smem);
+}
+
+cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threads, size_t smem,
+                               cudaStream_t stream)
+{
+    if (kind == 0)
+        qp3d_batch_plane_kernel<0><<<grid, threads, smem, stream>>>(b);
+    else if (kind == 1)
+        qp3d_batch_plane_kernel<1><<<grid, threads, smem, stream>>>(b);
+    else
+        qp3d_batch_plane_kernel<2><<<grid, threads, smem, stream>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,
+                               cudaStream_t stream)
+{
+    qp3d_batch_fixup_kernel<<<dim3(blocks_per_shot, nshots), 256, 0, stream>>>(b);
     return cudaGetLastError();
 }
 

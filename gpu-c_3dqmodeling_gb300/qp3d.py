@@ -34,6 +34,25 @@ class Model(ctypes.Structure):
                                       "ddlr", "dtb", "ddtb", "dfb", "ddfb", "c", "c2")]
 
 
+class ShotDesc(ctypes.Structure):
+    """qp3d_shot: one shot of qp3d_batch."""
+    _fields_ = [("geom", Geom), ("model", Model), ("record", _f32p)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("groups", ctypes.c_int), ("batched_shots", ctypes.c_int),
+                ("single_shots", ctypes.c_int), ("candidate", ctypes.c_int),
+                ("tile_rows", ctypes.c_int), ("zblocks", ctypes.c_int), ("tuned", ctypes.c_int),
+                ("ncand", ctypes.c_int), ("cand_ms", ctypes.c_float * 8),
+                ("graph_steps", ctypes.c_int), ("redo_steps", ctypes.c_int),
+                ("work_items", ctypes.c_int), ("ctas", ctypes.c_int), ("run_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "cand_ms"}
+        d["cand_ms"] = [round(float(v), 4) for v in self.cand_ms[:self.ncand]]
+        return d
+
+
 SNAP_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                            _f32p, ctypes.c_int, ctypes.c_int, ctypes.c_int)
 
@@ -75,7 +94,7 @@ class RunOptions(ctypes.Structure):
 # every symbol include/qp3d.h and include/qp3d_driver.h declare
 EXPORTS = [
     "qp3d_version", "qp3d_strerror", "qp3d_ctx_create", "qp3d_ctx_destroy",
-    "qp3d_ctx_last_error", "qp3d_forward", "qp3d_shot_load", "qp3d_shot_reset",
+    "qp3d_ctx_last_error", "qp3d_forward", "qp3d_batch", "qp3d_batch_get_stats", "qp3d_shot_load", "qp3d_shot_reset",
     "qp3d_shot_advance", "qp3d_shot_sync", "qp3d_shot_step", "qp3d_shot_read_record",
     "qp3d_shot_read_uxyzmax", "qp3d_shot_read_stats", "qp3d_shot_snapshot", "qp3d_pml_state_size",
     "qp3d_shot_write_state", "qp3d_shot_read_state", "qp3d_shot_time",
@@ -105,6 +124,8 @@ def load():
         "qp3d_ctx_destroy": (None, [_vp]),
         "qp3d_ctx_last_error": (ctypes.c_char_p, [_vp]),
         "qp3d_forward": (ctypes.c_int, [_vp, P(Geom), P(Model), _vp, P(Snap)]),
+        "qp3d_batch": (ctypes.c_int, [_vp, ctypes.c_int, P(ShotDesc)]),
+        "qp3d_batch_get_stats": (ctypes.c_int, [_vp, P(BatchStats)]),
         "qp3d_shot_load": (ctypes.c_int, [_vp, P(Geom), P(Model)]),
         "qp3d_shot_reset": (ctypes.c_int, [_vp]),
         "qp3d_shot_advance": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -329,6 +350,28 @@ class Context:
                                          _p(record), sp), "qp3d_forward")
         self._shot = shot
         return record
+
+    def batch(self, shots, records=None):
+        """Run many shots with qp3d_batch; returns their records."""
+        if records is None:
+            records = [np.empty((s.nt, s.hx, s.hy), np.float32) for s in shots]
+        arr = (ShotDesc * max(len(shots), 1))()
+        keep = []
+        for i, (s, r) in enumerate(zip(shots, records)):
+            if r.size != s.nt * s.hx * s.hy or r.dtype != np.float32 or not r.flags.c_contiguous:
+                raise ValueError("record %d must be a contiguous float32 array of nt*hx*hy" % i)
+            arr[i].geom = s.geom()
+            arr[i].model = s.model()
+            arr[i].record = r.ctypes.data_as(_f32p)
+            keep.append(r)
+        self._shot = None
+        self._check(self._L.qp3d_batch(self.h, len(shots), arr), "qp3d_batch")
+        return records
+
+    def batch_stats(self):
+        st = BatchStats()
+        self._check(self._L.qp3d_batch_get_stats(self.h, ctypes.byref(st)), "qp3d_batch_get_stats")
+        return st.as_dict()
 
     def load(self, shot, nt=None):
         g, m = shot.geom(nt), shot.model()

@@ -47,11 +47,10 @@ def linear_vti(h=100, nz0=100, pml=20, nt=1000, dx=10.0, dt=5e-4, fm=25.0, src=(
     return _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=src)
 
 
-def layered_vti(hx=400, hy=400, nz0=300, pml=30, nt=3000, dx=10.0, dt=5e-4, fm=20.0,
-                nlayers=12, seed=2, slope=0.15, src=None):
-    """Layered model with dipping planar interfaces: per layer vp U[1500,4500],
-    eps U[0,0.3], delta U[0,min(eps,0.15)].  Defaults: 400x400x300 interior,
-    30-cell PML, 3000 steps, 20 Hz source at the surface centre."""
+def layered_volume(hx, hy, nz0, nlayers=12, seed=2, slope=0.15):
+    """Interior vp, eps, delta ([nz0][hx][hy]) of a layered model with dipping
+    planar interfaces: per layer vp U[1500,4500], eps U[0,0.3],
+    delta U[0,min(eps,0.15)]."""
     rng = np.random.default_rng(seed)
     z0 = np.sort(rng.uniform(0, nz0, nlayers - 1))
     ax = rng.uniform(-slope, slope, nlayers - 1)
@@ -66,8 +65,50 @@ def layered_vti(hx=400, hy=400, nz0=300, pml=30, nt=3000, dx=10.0, dt=5e-4, fm=2
     for i in range(nlayers - 1):
         depth = z0[i] + ax[i] * xs + ay[i] * ys
         idx += (zz >= depth[None]).astype(np.int8)
-    vp_i, eps_i, del_i = lvp[idx], leps[idx], ldel[idx]
+    return lvp[idx], leps[idx], ldel[idx]
+
+
+def layered_vti(hx=400, hy=400, nz0=300, pml=30, nt=3000, dx=10.0, dt=5e-4, fm=20.0,
+                nlayers=12, seed=2, slope=0.15, src=None):
+    """Layered model (layered_volume).  Defaults: 400x400x300 interior,
+    30-cell PML, 3000 steps, 20 Hz source at the surface centre."""
+    vp_i, eps_i, del_i = layered_volume(hx, hy, nz0, nlayers, seed, slope)
     return _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=src)
+
+
+def batch_windows(nshots=64, seed=3, model=(512, 512, 200), hrange=(128, 256),
+                  zrange=(128, 200), frange=(15.0, 30.0)):
+    """Apertures of the batched workload: per shot (x0, y0, hx, hy, nz0, fm)
+    with hx, hy uniform in hrange, nz0 in zrange (inclusive), the window
+    origin uniform inside the model and the top of the window at the
+    surface."""
+    rng = np.random.default_rng(seed + 1000)
+    mx, my, mz = model
+    out = []
+    for _ in range(nshots):
+        hx = int(rng.integers(hrange[0], hrange[1] + 1))
+        hy = int(rng.integers(hrange[0], hrange[1] + 1))
+        nz0 = int(rng.integers(zrange[0], min(zrange[1], mz) + 1))
+        x0 = int(rng.integers(0, mx - hx + 1))
+        y0 = int(rng.integers(0, my - hy + 1))
+        fm = float(rng.uniform(*frange))
+        out.append((x0, y0, hx, hy, nz0, fm))
+    return out
+
+
+def batch_shots(nshots=64, seed=3, model=(512, 512, 200), pml=20, nt=2000, dx=10.0, dt=5e-4,
+                hrange=(128, 256), zrange=(128, 200), frange=(15.0, 30.0)):
+    """Batched workload: nshots windows (batch_windows) cut from one layered
+    model of the given interior size (layered_volume, 12 layers), each
+    extended by a pml-cell shell, with its Ricker source at the window's
+    surface centre and receivers on that plane."""
+    mx, my, mz = model
+    vp_m, eps_m, del_m = layered_volume(mx, my, mz, 12, seed, 0.15)
+    shots = []
+    for x0, y0, hx, hy, nz0, fm in batch_windows(nshots, seed, model, hrange, zrange, frange):
+        cut = lambda a: np.ascontiguousarray(a[:nz0, x0:x0 + hx, y0:y0 + hy])
+        shots.append(_finish(cut(vp_m), cut(eps_m), cut(del_m), pml, dx, dt, nt, fm))
+    return shots
 
 
 def small_case(hx=22, hy=26, nz0=18, pml=8, nt=60, seed=7, fm=30.0, src=None, dt=5e-4):

@@ -17,6 +17,9 @@
  *                             CPU impl modeling3D.c:17-153)
  *   qp3d_shot_* ............. the same call split into load / advance / read
  *                             so that callers can keep the model resident
+ *   qp3d_batch .............. the shot loop of the main programs
+ *                             (3dPureqPModeling1.0.c:225-277, Main.c:181-231),
+ *                             one modeling3d call per shot there
  *   qp3d_fdcoff1/2 .......... fdcoff1/fdcoff2, CPU_function.c:111-148
  *   qp3d_pmlcoff ............ pmlcoff, CPU_function.c:150-169
  *   qp3d_source ............. Source, CPU_function.c:37-64
@@ -95,6 +98,46 @@ const char *qp3d_ctx_last_error(const qp3d_ctx *ctx);
 int qp3d_forward(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m,
                  float *record, const qp3d_snap *snap);
 
+/* Many independent shots (each its own grid, model window, source, receiver
+ * depth and nt): the replacement of the main programs' loop of modeling3d
+ * calls.  Records are the same, bit for bit, as qp3d_forward's for each shot.
+ * All shots that fit in device memory are resident at once and every time
+ * step of all of them is one launch of a persistent kernel that takes work
+ * items (one tile column of one shot) from a device queue; steps after the
+ * first three are replayed from a captured CUDA graph.  The tile height and
+ * the number of z blocks per column are chosen by timing a few candidate
+ * shapes on the first steps of the run (results do not depend on the shape;
+ * the choice is cached per set of shot sizes).  Shots whose sources or
+ * receivers lie in the never-updated outer 5 cells, with more than 64 source
+ * cells, or with FD tables or spacings different from the first shot's run
+ * through qp3d_forward instead.  No snapshots.  Uses the context's stream and
+ * replaces any shot loaded with qp3d_shot_load. */
+typedef struct {
+    qp3d_geom geom;
+    qp3d_model model;
+    float *record;        /* out: nt*hx*hy floats, fully overwritten */
+} qp3d_shot;
+
+int qp3d_batch(qp3d_ctx *ctx, int nshots, const qp3d_shot *shots);
+
+typedef struct {
+    int groups;           /* groups of resident shots, run one after another */
+    int batched_shots;    /* shots run by the batched launches */
+    int single_shots;     /* shots run through qp3d_forward */
+    int candidate;        /* tile / z-block shape used in the last group */
+    int tile_rows;        /* its largest tile height (x rows per tile) */
+    int zblocks;          /* its z blocks per tile column */
+    int tuned;            /* 1: chosen by timing in this call */
+    int ncand;            /* candidates timed (tuned calls) */
+    float cand_ms[8];     /* mean step time of each candidate (tuned calls) */
+    int graph_steps;      /* steps replayed from the captured graph */
+    int redo_steps;       /* shot-steps whose speculation missed (re-run) */
+    int work_items;       /* work items per launch (last group) */
+    int ctas;             /* persistent CTAs per launch (last group) */
+    float run_ms;         /* device time of the time loop, summed over groups */
+} qp3d_batch_stats;
+int qp3d_batch_get_stats(const qp3d_ctx *ctx, qp3d_batch_stats *out);
+
 /* Staged form of the same shot. */
 int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m);
 int qp3d_shot_reset(qp3d_ctx *ctx);                 /* zero state, step 0 */
@@ -137,12 +180,18 @@ int qp3d_shot_time(qp3d_ctx *ctx, int nsteps, float *ms_total, float *ms_step,
 int qp3d_shot_launches_per_step(const qp3d_ctx *ctx);
 long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
 
-/* Launch tuning (autotuner hook).  Keys: "step_variant" (0: loads at use,
- * 1: next-plane prefetch), "gradmax_variant" (0: shared-memory z taps,
+/* Launch tuning.  Keys: "gradmax_variant" (0: shared-memory z taps,
  * 1: register queue), "tile_x" (rows per tile, 0 = automatic),
- * "chunks" (z chunks, 0 = automatic).  Takes effect at the next
- * qp3d_shot_load, or immediately for the loaded shot.  All settings compute
- * identical results. */
+ * "chunks" (z chunks, 0 = automatic), "threshold_mode" (0: gradmax pre-pass
+ * every step, 1: speculative threshold), "spec_delta_ppm" (smallest
+ * half-width of the predicted max window), "alt_cap" (deferred-cell list
+ * entries, 0 = automatic).  Single shots: takes effect at the next
+ * qp3d_shot_load, or immediately for the loaded shot.  qp3d_batch:
+ * "batch_graph" (1: replay steps from a captured graph), "batch_tune"
+ * (1: time the candidate shapes), "batch_candidate" (shape index used when
+ * not tuning, -1 = default), "batch_mem_mb" (device memory for one group of
+ * resident shots, 0 = what is free).  All settings compute identical
+ * results. */
 int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
 int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
 
