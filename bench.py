@@ -21,6 +21,16 @@ Metric: Gcell-updates/s = padded cells x time steps / seconds.
 
 --impl reference runs only that CPU implementation, a few time steps of the
 same workload per bench step.
+
+--workload batch measures the batched path instead (one bench step = one
+qp3d_batch call): 64 shots on uneven windows (hx, hy uniform in [128, 256],
+Nz0 in [128, 200], 20-cell PML, 10.8 M padded cells on average) cut from one
+512x512x200 layered model, 2000 steps, 15-30 Hz sources, surface receivers.
+  value      batched shots/s, device time of the time loop (all groups)
+  e2e        shots/s of the whole qp3d_batch call from pageable host buffers
+             (model upload, time loop, record download)
+  single_shot_form  the same shots one qp3d call each: device time of the
+             resident time loop and wall time of qp3d_forward
 """
 import argparse
 import json
@@ -58,6 +68,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="scale the horizontal/vertical extent (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="single", choices=["single", "batch"])
+    ap.add_argument("--shots", type=int, default=64, help="batch workload: shots")
     return ap.parse_args()
 
 
@@ -373,12 +385,111 @@ def run_gpu_arm(args, dist):
     return 0
 
 
+BATCH_NAME = ("%d shots, windows hx,hy U[128,256], Nz0 U[128,200] (+20-cell PML) cut from a "
+              "512x512x200 layered VTI model (12 dipping layers, seed 3), %d steps x 0.5 ms, "
+              "15-30 Hz Ricker at each window's surface centre, surface receivers")
+
+
+def run_batch_arm(args, dist):
+    import qp3d
+    import synthetic
+    nt = args.nt if args.nt is not None else 2000
+    shots = synthetic.batch_shots(nshots=args.shots, nt=nt)
+    cells = [s.N for s in shots]
+    work = sum(c * nt for c in cells)
+    ctx = qp3d.Context(dist.local)
+    records = [np.empty((s.nt, s.hx, s.hy), np.float32) for s in shots]
+    for _ in range(args.warmup):
+        ctx.batch(shots, records)
+    dist.barrier()
+    gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
+                 if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
+    clocks = Clocks(gpu_index)
+    launches0 = ctx.launch_count()
+    run_ms, wall = 0.0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.batch(shots, records)
+        wall += time.perf_counter() - t0
+        st = ctx.batch_stats()
+        run_ms += st["run_ms"]
+    clk = clocks.stop()
+    gpu_launches = ctx.launch_count() - launches0
+    run_ms = dist.max(run_ms)
+    wall = dist.max(wall)
+    n = dist.world * len(shots) * args.steps
+    value = n / (run_ms / 1e3)
+    e2e = n / wall
+
+    # the same shots one call each
+    ms_single, wall_single = 0.0, 0.0
+    for s in shots:
+        ctx.load(s)
+        ms_single += ctx.time(s.nt, per_kernel=False)[0]
+    t0 = time.perf_counter()
+    for s, r in zip(shots, records):
+        ctx.forward(s, record=r)
+    wall_single = time.perf_counter() - t0
+
+    # whole-step HBM rate of the batched time loop (algorithmic bytes of all
+    # shots per step / device time per step)
+    bsum = sum(algorithmic_bytes(s)[0] for s in shots)
+    peak, peak_kind = hbm_peak()
+    achieved = bsum / (run_ms / args.steps / nt / 1e3) / 1e9
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        secs, threads = cpu_sample(shots[0], CPU_SAMPLE_STEPS, k0=nt // 2)
+        rate = shots[0].N * CPU_SAMPLE_STEPS / secs
+        cpu = {"value": round(rate / (work / len(shots)), 6), "unit": "shots/s", "cores": threads,
+               "kind": "port",
+               "sample": "%d time steps of shot 0 (%dx%dx%d) from a dense random state, oracle "
+                         "port of CPU_function.c, OpenMP; shots/s = cell rate / mean cells x nt"
+                         % (CPU_SAMPLE_STEPS, shots[0].nx, shots[0].ny, shots[0].nz)}
+    if dist.rank == 0:
+        line = {
+            "metric": "batched shots/s", "value": round(value, 4), "unit": "shots/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(run_ms / args.steps, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": BATCH_NAME % (len(shots), nt),
+                       "step": "one qp3d_batch call over all shots",
+                       "shots": len(shots), "nt": nt, "cells_total": sum(cells),
+                       "cells_mean": round(sum(cells) / len(cells)),
+                       "l2": "inputs larger than L2 (working set %.0f GB)" %
+                             (sum(17 * c * 4 for c in cells) / 1e9),
+                       "parallelism": "replicas" if dist.world > 1 else "single"},
+            "gcell_per_s": round(dist.world * work * args.steps / (run_ms / 1e3) / 1e9, 3),
+            "step_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                              "unit": "GB/s", "frac": round(achieved / peak, 4),
+                              "note": "algorithmic bytes of all shots per time step / device "
+                                      "time per step (all kernels of the step)"},
+            "batch": st,
+            "single_shot_form": {
+                "value": round(len(shots) / (ms_single / 1e3), 4), "unit": "shots/s",
+                "e2e": round(len(shots) / wall_single, 4),
+                "note": "same shots, one call each: device time of the resident time loop "
+                        "(qp3d_shot_load + nt steps), and wall time of qp3d_forward"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e, 4), "unit": "shots/s",
+                    "h2d_bytes_per_step": sum(4 * (3 * c) + 4 * nt for c in cells),
+                    "d2h_bytes_per_step": sum(4 * nt * s.hx * s.hy for s in shots),
+                    "note": "pageable host buffers"},
+            "gpu_launches": gpu_launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.impl == "reference":
             return run_reference_arm(args, dist)
+        if args.workload == "batch":
+            return run_batch_arm(args, dist)
         return run_gpu_arm(args, dist)
     finally:
         dist.close()
