@@ -172,7 +172,7 @@ static void plan_launch(qp3d_ctx *ctx)
     if (ctx->tune_chunks > 0) nch = std::min(ctx->tune_chunks, ncz);
     ctx->chunk_z = (ncz + nch - 1) / nch;
     ctx->nchunks = (ncz + ctx->chunk_z - 1) / ctx->chunk_z;
-    ctx->smem = plane_smem_bytes(ctx->tile_x, g.pml);
+    ctx->smem = plane_smem_bytes(ctx->tile_x, g.pml, ctx->fuse_sources ? ctx->n_fused : 0);
 }
 
 static int alloc_vol(qp3d_ctx *ctx, float **p)
@@ -219,7 +219,6 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     ctx->vol = ctx->plane * g->nz;
     ctx->hx = g->nx - 2 * g->pml;
     ctx->hy = g->ny - 2 * g->pml;
-    plan_launch(ctx);
 
     if (!same) {
         float **vols[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->K,     &ctx->E2,
@@ -302,6 +301,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     // lies inside the updated box
     ctx->rec_fused = g->pml >= kRadius && g->sz >= kRadius && g->sz < g->nz - kRadius &&
                      ctx->fuse_sources && ctx->n_band == 0;
+    plan_launch(ctx);   // after the sources: the per-CTA source list is in shared memory
     for (int i = 0; i < 3; ++i)
         if ((rc = make_tmap(ctx, ctx->U[i], &ctx->tm[i]))) return rc;
     ctx->loaded = true;
@@ -391,21 +391,21 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
         p.alt_count = ctx->alt_count + k;
         p.alt_cap = ctx->alt_cap;
         if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
-        CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->step_variant));
+        CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
         if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
         if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
         CKL(launch_fixup(p, ctx->redo + k, ctx->spec_err, ctx->stream, ctx->nsm));
         PlaneParams pe = p;
         pe.spec = 0;
         pe.gate = ctx->redo + k;
-        CKL(launch_step(ctx->tm[a], pe, grid, ctx->smem, ctx->stream, ctx->step_variant));
+        CKL(launch_step(ctx->tm[a], pe, grid, ctx->smem, ctx->stream));
         if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
     } else {
         if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
         CKL(launch_gradmax(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->gradmax_variant));
         if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
         if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
-        CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream, ctx->step_variant));
+        CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
         if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
     }
     if (ctx->fuse_sources) {
@@ -775,8 +775,7 @@ extern "C" void qp3d_host_free(void *p)
 extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
 {
     if (!ctx || !key) return QP3D_ERR_ARG;
-    if (!strcmp(key, "step_variant") && (value == 0 || value == 1)) ctx->step_variant = value;
-    else if (!strcmp(key, "gradmax_variant") && (value == 0 || value == 1)) ctx->gradmax_variant = value;
+    if (!strcmp(key, "gradmax_variant") && (value == 0 || value == 1)) ctx->gradmax_variant = value;
     else if (!strcmp(key, "tile_x") && value >= 0 && value <= kMaxTileX) ctx->tune_tile_x = value;
     else if (!strcmp(key, "chunks") && value >= 0) ctx->tune_chunks = value;
     else if (!strcmp(key, "threshold_mode") && (value == 0 || value == 1)) ctx->threshold_mode = value;
@@ -814,7 +813,6 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
 extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
 {
     if (!ctx || !key) return QP3D_ERR_ARG;
-    if (!strcmp(key, "step_variant")) return ctx->step_variant;
     if (!strcmp(key, "gradmax_variant")) return ctx->gradmax_variant;
     if (!strcmp(key, "tile_x")) return ctx->loaded ? ctx->tile_x : ctx->tune_tile_x;
     if (!strcmp(key, "chunks")) return ctx->loaded ? ctx->nchunks : ctx->tune_chunks;

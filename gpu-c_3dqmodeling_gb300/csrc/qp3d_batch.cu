@@ -215,7 +215,7 @@ int Runner::build_candidate(int c, std::vector<Plan *> &G)
         const Plan &P = *G[s];
         const int tx = tile_height(P.g.nx, kCands[c].tile_rows);
         max_tile = std::max(max_tile, tx);
-        smem = std::max(smem, batch_smem_bytes(tx, P.g.pml));
+        smem = std::max(smem, batch_smem_bytes(tx, P.g.pml, (int)P.src.size()));
         const int nxt = (P.g.nx - 2 * kRadius + tx - 1) / tx;
         const int nyt = (P.g.ny - kRadius - 1) / kTileY + 1;
         const int ncz = P.g.nz - 2 * kRadius;

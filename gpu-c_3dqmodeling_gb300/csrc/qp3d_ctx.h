@@ -67,7 +67,7 @@ struct qp3d_ctx {
     cudaEvent_t ev[4] = {};
     cudaEvent_t uev[8] = {};
     // tuning
-    int step_variant = 0, gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
+    int gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
     int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
     float delta_min = 0.02f;         // smallest half-width of the predicted window
     unsigned tune_alt_cap = 0;

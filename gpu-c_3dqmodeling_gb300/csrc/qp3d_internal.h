@@ -24,7 +24,13 @@ constexpr int kTileY = 32;        // y cells per tile = 8 quads of 4 cells
 constexpr int kQuadsY = kTileY / 4;
 constexpr int kHaloY = 8;         // y halo rounded up to 16 bytes
 constexpr int kBoxY = kTileY + 2 * kHaloY;   // 48 floats per staged row
-constexpr int kPrefetch = 2;      // planes loaded ahead of use
+// Planes loaded ahead of use.  One is enough to cover the TMA latency; every
+// further slot costs 8 KB of shared memory per CTA, and the L1 share of the
+// SM (where the per-cell global loads wait for DRAM) shrinks with it: two
+// CTAs of 32-row tiles with a 12-slot ring fit the 196 KiB shared-memory
+// carveout (60 KiB left for L1), a 13-slot ring needs the 228 KiB carveout
+// (28 KiB of L1) and runs the step about 17% slower.
+constexpr int kPrefetch = 1;
 constexpr int kRing = 2 * kRadius + 1 + kPrefetch;   // staged planes
 constexpr int kMaxTileX = 32;
 constexpr int kThreads = kQuadsY * kMaxTileX;        // 256
@@ -147,7 +153,7 @@ struct Shot;   // host-side, defined in qp3d_api.cu
 cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p,
                            dim3 grid, size_t smem, cudaStream_t stream, int variant);
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p,
-                        dim3 grid, size_t smem, cudaStream_t stream, int variant);
+                        dim3 grid, size_t smem, cudaStream_t stream);
 cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
                          int nsm);
 cudaError_t launch_band_sources(float *u_new, const float *u_cur,
@@ -166,11 +172,13 @@ cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0,
 cudaError_t launch_params(const float *vp, const float *eps, const float *del,
                           float *K, float *E2, float *R8, long long n, float dt,
                           cudaStream_t stream);
-size_t plane_smem_bytes(int tile_x, int pml);
+// Dynamic shared memory of a plane kernel; nsrc = fused sources of the shot
+// (the per-CTA source list has room for all of them).
+size_t plane_smem_bytes(int tile_x, int pml, int nsrc = kMaxFusedSources);
 
 // Batched launches (persistent CTAs pulling work items).  kind: 0 gradmax,
 // 1 exact step (gated per shot), 2 speculative step.
-size_t batch_smem_bytes(int tile_x, int pml);
+size_t batch_smem_bytes(int tile_x, int pml, int nsrc);
 cudaError_t launch_batch_prepare(const BatchShot *shots, int nshots, PlaneParams *pp, int *ctr,
                                  int *queues, int spec, cudaStream_t stream);
 cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threads, size_t smem,

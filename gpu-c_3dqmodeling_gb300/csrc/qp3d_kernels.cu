@@ -133,7 +133,8 @@ struct SmemLayout {
     size_t total;
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int tile_x, int pml)
+__host__ __device__ inline SmemLayout smem_layout(int tile_x, int pml,
+                                                  int nsrc = kMaxFusedSources)
 {
     SmemLayout L;
     size_t box = (size_t)(tile_x + 2 * kRadius) * kBoxY;
@@ -143,13 +144,13 @@ __host__ __device__ inline SmemLayout smem_layout(int tile_x, int pml)
     L.tab_off = L.bar_off + 16 * kRing;   // full[kRing], empty[kRing]
     L.tab_off = (L.tab_off + 15) & ~(size_t)15;
     L.src_off = L.tab_off + 16 * 3 * (size_t)(pml > 0 ? pml : 1);
-    L.misc_off = L.src_off + sizeof(SrcEntry) * kMaxFusedSources;
+    L.misc_off = L.src_off + sizeof(SrcEntry) * (size_t)(nsrc > 0 ? nsrc : 1);
     L.misc_off = (L.misc_off + 15) & ~(size_t)15;
     L.total = L.misc_off + 64;
     return L;
 }
 
-size_t plane_smem_bytes(int tile_x, int pml) { return smem_layout(tile_x, pml).total; }
+size_t plane_smem_bytes(int tile_x, int pml, int nsrc) { return smem_layout(tile_x, pml, nsrc).total; }
 
 // ---------------------------------------------------------------------------
 // Threshold of the scalar operator, GPU_kernel.cu:99.
@@ -793,7 +794,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                                           const Coefs &k, int tile_x, int y0, int x0, int z0,
                                           int z1, bool win_writer, unsigned char *smem)
 {
-    const SmemLayout L = smem_layout(tile_x, p.pml);
+    const SmemLayout L = smem_layout(tile_x, p.pml, p.nsrc);
     float4 *tab = reinterpret_cast<float4 *>(smem + L.tab_off);
     SrcEntry *csrc = reinterpret_cast<SrcEntry *>(smem + L.src_off);
     float *misc = reinterpret_cast<float *>(smem + L.misc_off);
@@ -828,7 +829,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         for (int e = 0; e < p.nsrc; ++e) {
             SrcEntry s = p.src[e];
             if (s.x >= x0 && s.x < x0 + tile_x && s.y >= y0 && s.y < y0 + kTileY && s.z >= z0 &&
-                s.z < z1 && n < kMaxFusedSources)
+                s.z < z1 && n < p.nsrc)
                 csrc[n++] = s;
         }
         misc_i[0] = n;
@@ -1287,7 +1288,10 @@ __global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, Pl
 
 constexpr size_t kParamBytes = (sizeof(PlaneParams) + 127) & ~(size_t)127;
 
-size_t batch_smem_bytes(int tile_x, int pml) { return kParamBytes + plane_smem_bytes(tile_x, pml); }
+size_t batch_smem_bytes(int tile_x, int pml, int nsrc)
+{
+    return kParamBytes + plane_smem_bytes(tile_x, pml, nsrc);
+}
 
 // KIND 0: gradmax, 1: exact step (skipped for shots whose gate is 0),
 // 2: speculative step.
@@ -1395,13 +1399,12 @@ cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 g
 }
 
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
-                        cudaStream_t stream, int variant)
+                        cudaStream_t stream)
 {
     if (p.spec)
         qp3d_step_kernel<true><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
     else
         qp3d_step_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
-    (void)variant;
     return cudaGetLastError();
 }
 
