@@ -11,6 +11,7 @@
 #include "qp3d_ctx.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -44,18 +45,22 @@ static void free_shot(qp3d_ctx *ctx)
                       &ctx->R8,    &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0],
                       &ctx->W3[1], &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],
                       &ctx->W21[0], &ctx->W21[1], &ctx->record, &ctx->gmax, &ctx->snap_dev,
-                      &ctx->win,   &ctx->spec_err};
+                      &ctx->win,   &ctx->spec_err, &ctx->am2, &ctx->av, &ctx->sres};
     for (float **b : bufs) {
         if (*b) cudaFree(*b);
         *b = nullptr;
     }
     if (ctx->redo) cudaFree(ctx->redo);
     if (ctx->alt_count) cudaFree(ctx->alt_count);
-    if (ctx->alt) cudaFree(ctx->alt);
+    if (ctx->amask) cudaFree(ctx->amask);
+    if (ctx->alist) cudaFree(ctx->alist);
+    if (ctx->fix_count) cudaFree(ctx->fix_count);
+    ctx->fix_count = nullptr;
     ctx->redo = nullptr;
     ctx->alt_count = nullptr;
-    ctx->alt = nullptr;
-    ctx->alt_cap = 0;
+    ctx->amask = nullptr;
+    ctx->alist = nullptr;
+    ctx->alist_cap = 0;
     if (ctx->layers) cudaFree(ctx->layers);
     if (ctx->src_fused) cudaFree(ctx->src_fused);
     if (ctx->src_band) cudaFree(ctx->src_band);
@@ -240,10 +245,17 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         CK(cudaMalloc(&ctx->redo, ntb * sizeof(int)));
         CK(cudaMalloc(&ctx->alt_count, ntb * sizeof(unsigned)));
         CK(cudaMalloc(&ctx->spec_err, sizeof(float)));
-        long long cap = ctx->tune_alt_cap ? (long long)ctx->tune_alt_cap
-                                          : std::max(1ll << 20, ctx->vol / 4);
-        ctx->alt_cap = (unsigned)std::min(cap, (long long)0x7fffffff);
-        CK(cudaMalloc(&ctx->alt, (size_t)ctx->alt_cap * sizeof(AltEntry)));
+        // deferred cells of a speculative step: one bit per cell (vol is a
+        // multiple of 32), m2 and the alternative value at the cell's index
+        CK(cudaMalloc(&ctx->amask, (size_t)defer_mask_words(ctx->vol) * sizeof(unsigned)));
+        CK(cudaMalloc(&ctx->am2, (size_t)ctx->vol * sizeof(float)));
+        CK(cudaMalloc(&ctx->av, (size_t)ctx->vol * sizeof(float)));
+        CK(cudaMalloc(&ctx->fix_count, ntb * sizeof(unsigned)));
+        CK(cudaMalloc(&ctx->sres, 2 * ntb * sizeof(float)));
+        // compacted list: a quarter of the cells (more deferred cells than
+        // that make the step re-run exactly)
+        ctx->alist_cap = (unsigned)std::min<long long>(std::max(1ll << 16, ctx->vol / 4), 0x7fffffff);
+        CK(cudaMalloc(&ctx->alist, (size_t)ctx->alist_cap * sizeof(unsigned)));
     }
     // model -> per-cell parameters (K, E2, R8 hold vp, eps, delta first)
     if ((rc = upload_vol(ctx, ctx->K, m->vp)) || (rc = upload_vol(ctx, ctx->E2, m->epsilon)) ||
@@ -322,6 +334,9 @@ extern "C" int qp3d_shot_reset(qp3d_ctx *ctx)
     CK(cudaMemsetAsync(ctx->win, 0, 3 * ntb * sizeof(float), ctx->stream));
     CK(cudaMemsetAsync(ctx->redo, 0, ntb * sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->alt_count, 0, ntb * sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->fix_count, 0, ntb * sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->amask, 0, (size_t)defer_mask_words(ctx->vol) * sizeof(unsigned),
+                       ctx->stream));
     static const float one = 1.0f;
     CK(cudaMemcpyAsync(ctx->spec_err, &one, sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(ctx->gmax, 0, sizeof(float) * std::max(ctx->g.nt, 1), ctx->stream));
@@ -387,14 +402,21 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
         p.spec = 1;
         p.win = ctx->win + 3 * (size_t)k;
         p.spec_err = ctx->spec_err;
-        p.alt = ctx->alt;
+        p.spec_bias = ctx->spec_bias;
+        p.amask = ctx->amask;
+        p.am2 = ctx->am2;
+        p.av = ctx->av;
         p.alt_count = ctx->alt_count + k;
-        p.alt_cap = ctx->alt_cap;
+        p.alist = ctx->alist;
+        p.alist_cap = ctx->alist_cap;
+        p.fix_count = ctx->fix_count + k;
+        p.sres = ctx->sres + 2 * (size_t)k;
         if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
         CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
         if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
         if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
         CKL(launch_fixup(p, ctx->redo + k, ctx->spec_err, ctx->stream, ctx->nsm));
+        ctx->launches += 2;   // resolution, compaction, fix-up
         PlaneParams pe = p;
         pe.spec = 0;
         pe.gate = ctx->redo + k;
@@ -428,7 +450,7 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
 extern "C" int qp3d_shot_launches_per_step(const qp3d_ctx *ctx)
 {
     if (!ctx || !ctx->loaded) return 0;
-    int n = use_spec(ctx, ctx->step) ? 3 : 2;
+    int n = use_spec(ctx, ctx->step) ? 5 : 2;   // step, resolution, compaction, fix-up, re-run
     if (ctx->fuse_sources) n += ctx->n_band > 0 ? 1 : 0;
     else n += ctx->n_all > 0 ? 1 : 0;
     if (!ctx->rec_fused) n += 1;
@@ -786,18 +808,8 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "batch_candidate") && value >= -1 && value < 16)
         ctx->batch_candidate = value;
     else if (!strcmp(key, "batch_mem_mb") && value >= 0) ctx->batch_mem_mb = value;
-    else if (!strcmp(key, "alt_cap") && value >= 0) {
-        ctx->tune_alt_cap = (unsigned)value;
-        if (ctx->loaded) {
-            CK(cudaSetDevice(ctx->device));
-            CK(cudaStreamSynchronize(ctx->stream));
-            if (ctx->alt) cudaFree(ctx->alt);
-            ctx->alt = nullptr;
-            long long cap = value ? (long long)value : std::max(1ll << 20, ctx->vol / 4);
-            ctx->alt_cap = (unsigned)std::min(cap, (long long)0x7fffffff);
-            CK(cudaMalloc(&ctx->alt, (size_t)std::max(ctx->alt_cap, 1u) * sizeof(AltEntry)));
-        }
-    }
+    else if (!strcmp(key, "spec_bias_ppm") && value >= -500000 && value <= 1000000)
+        ctx->spec_bias = value * 1e-6f;
     else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
     if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
         CK(cudaSetDevice(ctx->device));
@@ -818,7 +830,7 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "chunks")) return ctx->loaded ? ctx->nchunks : ctx->tune_chunks;
     if (!strcmp(key, "threshold_mode")) return ctx->threshold_mode;
     if (!strcmp(key, "spec_delta_ppm")) return (int)(ctx->delta_min * 1e6f + 0.5f);
-    if (!strcmp(key, "alt_cap")) return (int)ctx->alt_cap;
+    if (!strcmp(key, "spec_bias_ppm")) return (int)lrintf(ctx->spec_bias * 1e6f);
     if (!strcmp(key, "batch_graph")) return ctx->batch_graph;
     if (!strcmp(key, "batch_tune")) return ctx->batch_tune;
     if (!strcmp(key, "batch_candidate")) return ctx->batch_candidate;

@@ -48,7 +48,6 @@ struct Plan {
     int ldy = 0, hx = 0, hy = 0;
     long long plane = 0, vol = 0;
     std::vector<SrcEntry> src;
-    unsigned alt_cap = 0;
     size_t bytes = 0;               // device bytes of this shot
     BatchShot d{};                  // device pointers, filled per group
 };
@@ -119,12 +118,18 @@ void carve(Plan &s, Carver &c, size_t *zero_bytes)
     d.win = c.take<float>(3 * nt);
     d.redo = c.take<int>(nt);
     d.alt_count = c.take<unsigned>(nt);
+    d.fix_count = c.take<unsigned>(nt);
+    d.sres = c.take<float>(2 * nt);
+    d.amask = c.take<unsigned>((size_t)defer_mask_words((long long)vol));
     if (zero_bytes) *zero_bytes = c.off - start;
     d.K = c.take<float>(vol);
     d.E2 = c.take<float>(vol);
     d.R8 = c.take<float>(vol);
     d.spec_err = c.take<float>(1);
-    d.alt = c.take<AltEntry>(std::max(s.alt_cap, 1u));
+    d.am2 = c.take<float>(vol);
+    d.av = c.take<float>(vol);
+    d.alist_cap = (unsigned)std::min<size_t>(std::max<size_t>(1u << 16, vol / 4), 0x7fffffff);
+    d.alist = c.take<unsigned>(d.alist_cap);
     d.layers = c.take<float4>(3 * (size_t)std::max(s.g.pml, 1));
     d.wavelet = c.take<float>(nt);
     d.src = c.take<SrcEntry>(std::max<size_t>(s.src.size(), 1));
@@ -188,6 +193,7 @@ class Runner {
     BatchState *B;
     Launch L[kNumCands];
     int nshots = 0;
+    long long max_words = 0;   // largest deferred-cell bitmask of the group
     Coefs coefs{};
 
     int build_candidate(int c, std::vector<Plan *> &G);
@@ -269,7 +275,8 @@ int Runner::enqueue_step(int c, bool spec)
     if (spec) {
         CKL(launch_batch_plane(2, args(c, 1), l.grid, l.threads, l.smem, ctx->stream));
         const int per_shot = std::max(2, 8 * ctx->nsm / std::max(nshots, 1));
-        CKL(launch_batch_fixup(args(c, 1), nshots, per_shot, ctx->stream));
+        CKL(launch_batch_fixup(args(c, 1), nshots, per_shot, max_words, ctx->stream));
+        ctx->launches += 2;   // resolution, compaction, fix-up
         CKL(launch_batch_plane(1, args(c, 2), l.grid, l.threads, l.smem, ctx->stream));
     } else {
         CKL(launch_batch_plane(0, args(c, 0), l.grid, l.threads, l.smem, ctx->stream));
@@ -283,6 +290,8 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
     int rc;
     nshots = (int)G.size();
     coefs = kc;
+    max_words = 0;
+    for (Plan *p : G) max_words = std::max(max_words, defer_mask_words(p->vol));
     // ---- device memory: one arena for the group
     size_t total = 0;
     for (Plan *p : G) total += p->bytes;
@@ -323,7 +332,7 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
         d.dt = P.g.dt;
         d.delta_min = ctx->delta_min;
         d.nsrc = (int)P.src.size();
-        d.alt_cap = P.alt_cap;
+        d.spec_bias = ctx->spec_bias;
         d.err = ctx->errword;
         nt_max = std::max(nt_max, P.g.nt);
         CK(cudaMemsetAsync(static_cast<char *>(B->arena) + start, 0, zero_bytes, ctx->stream));
@@ -561,9 +570,6 @@ extern "C" int qp3d_batch(qp3d_ctx *ctx, int nshots, const qp3d_shot *shots)
                 }
         }
         derive_coefs(m.c, m.c2, g.dx, g.dy, g.dz, &coefs[i]);
-        P.alt_cap = ctx->tune_alt_cap
-                        ? ctx->tune_alt_cap
-                        : (unsigned)std::min<long long>(std::max(1ll << 16, P.vol / 16), 0x7fffffff);
         Carver cv{nullptr};
         carve(P, cv, nullptr);
         P.bytes = cv.off;

@@ -47,8 +47,12 @@ struct qp3d_ctx {
     int *redo = nullptr;
     unsigned *alt_count = nullptr;
     float *spec_err = nullptr;
-    qp3d::AltEntry *alt = nullptr;
-    unsigned alt_cap = 0;
+    unsigned *amask = nullptr;       // deferred-cell bits, vol / 32 words
+    float *am2 = nullptr, *av = nullptr;
+    unsigned *fix_count = nullptr;   // per step: deferred cells below the threshold
+    float *sres = nullptr;           // per step: T2 and the window hit
+    unsigned *alist = nullptr;       // compacted deferred cells
+    unsigned alist_cap = 0;
     float4 *layers = nullptr;
     qp3d::SrcEntry *src_fused = nullptr, *src_band = nullptr, *src_all = nullptr;
     int n_fused = 0, n_band = 0, n_all = 0;
@@ -69,8 +73,8 @@ struct qp3d_ctx {
     // tuning
     int gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
     int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
-    float delta_min = 0.02f;         // smallest half-width of the predicted window
-    unsigned tune_alt_cap = 0;
+    float delta_min = 0.01f;         // smallest half-width of the predicted window
+    float spec_bias = 0.0f;          // test hook: shifts the predicted window
     long long launches = 0;          // kernels launched by this context
     // batched shots (qp3d_batch)
     qp3d::BatchState *batch = nullptr;

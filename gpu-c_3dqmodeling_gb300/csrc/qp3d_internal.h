@@ -56,14 +56,10 @@ struct SrcEntry {
     float v;
 };
 
-// One cell whose threshold decision waited for the exact max of the step.
-struct AltEntry {
-    unsigned idx;        // pitched cell index
-    float m2;            // |grad u|^2 as the kernel computed it
-    float v;             // interior cell: its u(k+1) with S = 1 (source included);
-                         // PML cell: the source term added to it (flags bit 0)
-    unsigned flags;      // bit 0: source added, bit 1: PML cell (recomputed)
-};
+// Words of the deferred-cell bitmask of a volume of vol cells (vol is a
+// multiple of 32), rounded up to a multiple of 4 for 16-byte loads; the
+// padding words stay zero.
+__host__ __device__ inline long long defer_mask_words(long long vol) { return ((vol >> 5) + 3) & ~3ll; }
 
 struct PlaneParams {
     // geometry
@@ -92,14 +88,24 @@ struct PlaneParams {
     int nsrc;
     unsigned *err;
     // threshold handling of the step kernel
-    int spec;                 // 1: predicted window, own max, alternatives list
+    int spec;                 // 1: predicted window, own max, deferred cells
     const int *gate;          // exact mode: run only if *gate != 0 (null: always)
     float *win;               // spec: &win[3*step] = (M_lo, M_hi, M_pred)
     const float *spec_err;    // last relative prediction error of the max
     float delta_min;          // smallest half-width of the window
-    AltEntry *alt;            // alternatives of this step
-    unsigned *alt_count;      // &alt_count[step]
-    unsigned alt_cap;
+    float spec_bias;          // relative shift of the window (test hook, 0)
+    // Cells whose decision waits for the exact max of the step ("deferred"):
+    // one bit per cell, 32 y-cells per word (word = pitched index / 32), and
+    // at the cell's own index its m2 and its alternative value -- interior
+    // cell: u(k+1) with S = 1 (source included); PML cells are recomputed by
+    // the fix-up.
+    unsigned *amask;
+    float *am2, *av;
+    unsigned *alt_count;      // &alt_count[step]: deferred cells (compaction)
+    unsigned *fix_count;      // &fix_count[step]: of them below the threshold
+    float *sres;              // &sres[2*step]: T2 of the true max, 1 if inside the window
+    unsigned *alist;          // their pitched indices (compaction -> fix-up)
+    unsigned alist_cap;
     // batched launches only
     int ucur;                 // index of u(k) among the shot's three buffers
     int active;               // 0 once the shot has run all its steps
@@ -125,8 +131,13 @@ struct BatchShot {
     int *redo;                // nt
     unsigned *alt_count;      // nt
     float *spec_err;
-    AltEntry *alt;
-    unsigned alt_cap;
+    unsigned *amask;          // vol / 32 words
+    float *am2, *av;          // vol each
+    unsigned *fix_count;      // nt
+    float *sres;              // 2 * nt
+    unsigned *alist;          // alist_cap entries
+    unsigned alist_cap;
+    float spec_bias;
     unsigned *err;
 };
 
@@ -154,6 +165,8 @@ cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p,
                            dim3 grid, size_t smem, cudaStream_t stream, int variant);
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p,
                         dim3 grid, size_t smem, cudaStream_t stream);
+// Speculative step resolution: compaction of the deferred-cell bitmask into a
+// list, then the fix-up of the listed cells.
 cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
                          int nsm);
 cudaError_t launch_band_sources(float *u_new, const float *u_cur,
@@ -184,7 +197,7 @@ cudaError_t launch_batch_prepare(const BatchShot *shots, int nshots, PlaneParams
 cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threads, size_t smem,
                                cudaStream_t stream);
 cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,
-                               cudaStream_t stream);
+                               long long max_words, cudaStream_t stream);
 int batch_plane_threads(int tile_x);
 cudaError_t batch_ctas_per_sm(int kind, int threads, size_t smem, int *n);
 cudaError_t configure_gradmax_partial();

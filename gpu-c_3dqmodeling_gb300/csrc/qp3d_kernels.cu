@@ -30,8 +30,10 @@
 // dx*dx, CPU_function.c:314-316,393-395) are folded into the coefficient
 // tables, and a*b+c is fused where written as fmaf().  This translation unit
 // is compiled with -fmad=false so that no other fusion happens: the result is
-// bit-identical to the mirror variant of the CPU oracle.  Division and square
-// root are IEEE (div.rn / sqrt.rn).
+// bit-identical to the mirror variant of the CPU oracle.  The two divisions of
+// the scalar operator are Newton-Raphson reciprocals (rcp_nr: fused
+// multiply-adds only, so the oracle reproduces them exactly); the square root
+// is IEEE (sqrt.rn).
 #include "qp3d_internal.h"
 
 #include <math.h>
@@ -773,16 +775,40 @@ __device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &p
     const float d = fminf(0.25f, fmaxf(p.delta_min, __fmul_rn(3.0f, *p.spec_err)));
     lo = __fmul_rn(fminf(pred, m1), __fsub_rn(1.0f, d));
     hi = __fmul_rn(fmaxf(pred, m1), __fadd_rn(1.0f, d));
+    if (p.spec_bias != 0.0f) {   // test hook: a window that misses on purpose
+        lo = __fmul_rn(lo, __fadd_rn(1.0f, p.spec_bias));
+        hi = __fmul_rn(hi, __fadd_rn(1.0f, p.spec_bias));
+    }
 }
 
-// S of one cell (GPU_kernel.cu:100-111), given it is above the threshold.
+// 1/x for normal positive x, within about 1 ulp: Newton-Raphson steps
+// r <- r + r (1 - x r) from an initial guess that negates the exponent of x in
+// its integer representation (the integer-subtraction trick known from the
+// fast inverse square root).  Three steps take the guess's ~12% error below
+// float rounding.  About a third of the instructions of an IEEE division,
+// which dominated the scalar operator once most cells are above the
+// threshold; the mirror oracle performs the same operations.
+__device__ __forceinline__ float rcp_nr(float x)
+{
+    float r = __uint_as_float(0x7EF311C3u - __float_as_uint(x));
+#pragma unroll
+    for (int it = 0; it < 3; ++it) {
+        const float e = fmaf(-x, r, 1.0f);
+        r = fmaf(r, e, r);
+    }
+    return r;
+}
+
+// S of one cell (GPU_kernel.cu:100-111), given it is above the threshold:
+// with a = (nx^2 + ny^2) = h2/m2 and nz^2 = 1 - a,
+// S = 1/2 + 1/2 sqrt(1 - 8(eps-delta) a (1-a) / (1 + 2 eps a)^2).
 __device__ __forceinline__ float aniso_s(float h2, float m2, float e2x, float r8)
 {
-    float aa = __fdiv_rn(h2, m2);
+    float aa = __fmul_rn(h2, rcp_nr(m2));
     float bb = __fsub_rn(1.0f, aa);
     float den = fmaf(e2x, aa, 1.0f);
     float num = __fmul_rn(__fmul_rn(r8, aa), bb);
-    float qq = __fdiv_rn(num, __fmul_rn(den, den));
+    float qq = __fmul_rn(num, rcp_nr(__fmul_rn(den, den)));
     return fmaf(0.5f, __fsqrt_rn(__fsub_rn(1.0f, qq)), 0.5f);
 }
 
@@ -923,7 +949,6 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
 #pragma unroll
         for (int j = 0; j < 4; ++j) e2[j] = __fadd_rn(1.0f, f4(Ev, j));
         float out[4], alt[4];
-        bool cell_pml[4] = {false, false, false, false};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
@@ -944,7 +969,6 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                                          f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
                                          n13[j], n21[j], n33[j], n3[j]);
                 out[j] = is_pml ? v : out[j];
-                cell_pml[j] = is_pml;
                 n13[j] = is_pml ? n13[j] : 0.0f;
                 n33[j] = is_pml ? n33[j] : 0.0f;
                 n3[j] = is_pml ? n3[j] : 0.0f;
@@ -958,8 +982,6 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
             }
         }
         // source injection (GPU_kernel.cu:727): u3 += source * wavelet
-        float sadd[4] = {0.f, 0.f, 0.f, 0.f};
-        unsigned sflag = 0;
         for (int e = 0; e < ncsrc; ++e) {
             const SrcEntry s = csrc[e];
             if (s.z == z && s.x == x) {
@@ -970,8 +992,6 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                     if (jj == js) {
                         out[jj] = __fadd_rn(out[jj], add);
                         alt[jj] = __fadd_rn(alt[jj], add);
-                        sadd[jj] = add;
-                        sflag |= 1u << jj;
                     }
             }
         }
@@ -989,35 +1009,21 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                 }
             }
         }
-        // uncertain cells, appended warp-wide (all lanes take part)
+        // deferred cells: the row's bitmask word (the 8 lanes of a row combine
+        // their 4 bits; written every step, so stale bits never survive), and
+        // for a quad with any deferred cell its m2 and S = 1 values
         if (SPEC) {
-            const int cnt = (int)amb[0] + (int)amb[1] + (int)amb[2] + (int)amb[3];
-            if (__any_sync(0xffffffffu, cnt > 0)) {
-                int incl = cnt;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += v;
-                }
-                const int total = __shfl_sync(0xffffffffu, incl, 31);
-                unsigned wbase = 0;
-                if (lane == 31) wbase = atomicAdd(p.alt_count, (unsigned)total);
-                wbase = __shfl_sync(0xffffffffu, wbase, 31);
-                unsigned pos = wbase + (unsigned)(incl - cnt);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (!amb[j]) continue;
-                    if (pos < p.alt_cap) {
-                        AltEntry e;
-                        e.idx = (unsigned)(base + j);
-                        e.m2 = m2[j];
-                        e.v = cell_pml[j] ? sadd[j] : alt[j];
-                        e.flags = ((sflag >> j) & 1u) | (cell_pml[j] ? 2u : 0u);
-                        p.alt[pos] = e;
-                    }
-                    ++pos;
-                }
+            const unsigned nib = (unsigned)amb[0] | ((unsigned)amb[1] << 1) |
+                                 ((unsigned)amb[2] << 2) | ((unsigned)amb[3] << 3);
+            if (nib) {
+                *reinterpret_cast<float4 *>(p.am2 + base) = make_float4(m2[0], m2[1], m2[2], m2[3]);
+                *reinterpret_cast<float4 *>(p.av + base) = make_float4(alt[0], alt[1], alt[2], alt[3]);
             }
+            unsigned w = nib << (4 * q);
+            w |= __shfl_xor_sync(0xffffffffu, w, 1);
+            w |= __shfl_xor_sync(0xffffffffu, w, 2);
+            w |= __shfl_xor_sync(0xffffffffu, w, 4);
+            if (q == 0 && row_ok) p.amask[base >> 5] = w;
         }
         pipe_release(P, t);
     }
@@ -1028,7 +1034,8 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
     if (SPEC) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0 && mx > 0.0f)
+        if (lane == 0 && mx > 0.0f &&
+            mx > *reinterpret_cast<const volatile float *>(p.gmax + p.step))
             atomicMax(reinterpret_cast<unsigned *>(p.gmax + p.step), __float_as_uint(mx));
     }
     if (REUSE) {
@@ -1080,54 +1087,135 @@ __device__ void cell_derivs(const float *u, long long i, long long sx, long long
     Uxx = l[0]; Uyy = l[1]; Uzz = l[2];
 }
 
-// Resolves a speculative step.  If the true max lies in the window and the
-// list did not overflow, every listed cell that is below the true threshold
-// is recomputed with S = 1 from the step's (untouched) inputs; otherwise
-// *redo = 1 and the gated exact re-run recomputes the whole step.  Also
-// records the relative error of the prediction.
-__device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k, int *redo,
-                                           float *spec_err, unsigned block, unsigned nblocks)
+// Resolution of a speculative step, one thread: whether the true max fell in
+// the predicted window, the threshold T2 of the true max, the re-run flag and
+// the relative error of the prediction.
+__device__ __forceinline__ void resolve_body(const PlaneParams &p, int *redo, float *spec_err)
 {
     const float M = p.gmax[p.step];
     const float lo = p.win[0], hi = p.win[1], pred = p.win[2];
-    const unsigned n = *p.alt_count;
-    const bool inside = (M >= lo) && (M <= hi) && (n <= p.alt_cap);
-    if (block == 0 && threadIdx.x == 0) {
-        *redo = inside ? 0 : 1;
-        *spec_err = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
-    }
-    if (!inside) return;
-    const float T2 = threshold_m2(M);
-    const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml, hy = ny - 2 * pml;
-    for (unsigned i = block * blockDim.x + threadIdx.x; i < n; i += nblocks * blockDim.x) {
-        const AltEntry e = p.alt[i];
-        if (e.m2 > T2) continue;
-        const long long idx = e.idx;
-        const int z = (int)(idx / p.plane);
-        const long long rem = idx % p.plane;
-        const int x = (int)(rem / p.ldy), y = (int)(rem % p.ldy);
-        if (!(e.flags & 2u)) {   // interior cell: its S = 1 value came with the entry
-            p.u_out[idx] = e.v;
-            if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
-                p.record[(long long)(x - pml) * hy + (y - pml)] = e.v;
-            continue;
+    const bool inside = (M >= lo) && (M <= hi);
+    p.sres[0] = threshold_m2(M);
+    p.sres[1] = inside ? 1.0f : 0.0f;
+    *redo = inside ? 0 : 1;   // the fix-up sets it too when the list overflows
+    *spec_err = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
+}
+
+__global__ void qp3d_resolve_kernel(const PlaneParams p, int *redo, float *spec_err)
+{
+    if (threadIdx.x == 0) resolve_body(p, redo, spec_err);
+}
+
+// Compaction of the deferred-cell bitmask, four words per thread, one global
+// atomic per block and counter.  *p.alt_count ends as the number of deferred
+// cells of the step; when the true max lies in the predicted window, the
+// cells that are below the true threshold (m2 <= T2) are listed in p.alist
+// and counted in *p.fix_count.
+__device__ __forceinline__ void compact_body(const PlaneParams &p, unsigned block)
+{
+    __shared__ unsigned s_warp[32], s_def[32];
+    __shared__ unsigned s_base;
+    const float T2 = p.sres[0];
+    const bool inside = p.sres[1] != 0.0f;
+    const unsigned nwords = (unsigned)defer_mask_words(p.plane * p.nz);   // a multiple of 4
+    const unsigned w0 = (block * blockDim.x + threadIdx.x) * 4u;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint4 wv = make_uint4(0u, 0u, 0u, 0u);
+    if (w0 < nwords) wv = *reinterpret_cast<const uint4 *>(p.amask + w0);
+    const unsigned ws[4] = {wv.x, wv.y, wv.z, wv.w};
+    unsigned fix[4] = {0u, 0u, 0u, 0u};
+    unsigned c = 0, dcnt = 0;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        const unsigned w = ws[h];
+        dcnt += __popc(w);
+        if (w && inside) {
+            const float4 *m = reinterpret_cast<const float4 *>(p.am2 + (size_t)(w0 + h) * 32);
+#pragma unroll
+            for (int q4 = 0; q4 < 8; ++q4) {
+                const unsigned nib = (w >> (4 * q4)) & 15u;
+                if (!nib) continue;
+                const float4 v = m[q4];
+                const unsigned below = (unsigned)!(v.x > T2) | ((unsigned)!(v.y > T2) << 1) |
+                                       ((unsigned)!(v.z > T2) << 2) | ((unsigned)!(v.w > T2) << 3);
+                fix[h] |= (nib & below) << (4 * q4);
+            }
         }
-        float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
-        cell_derivs(p.u_cur, idx, p.ldy, p.plane, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
-        const float K = p.prm_k[idx];
-        const float KS = __fmul_rn(K, 1.0f);
-        const float e2 = __fadd_rn(1.0f, p.prm_e[idx]);
-        float out;
+        c += __popc(fix[h]);
+    }
+    unsigned incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += v;
+        dcnt += __shfl_xor_sync(0xffffffffu, dcnt, o);
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    if (lane == 0) s_def[warp] = dcnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0, d = 0;
+        for (unsigned i = 0; i < (blockDim.x >> 5); ++i) {
+            const unsigned v = s_warp[i];
+            s_warp[i] = t;
+            t += v;
+            d += s_def[i];
+        }
+        if (d) atomicAdd(p.alt_count, d);
+        s_base = t ? atomicAdd(p.fix_count, t) : 0u;
+    }
+    __syncthreads();
+    unsigned pos = s_base + s_warp[warp] + incl - c;
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        unsigned bits = fix[h];
+        while (bits) {
+            const int bit = __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (pos < p.alist_cap) p.alist[pos] = (w0 + h) * 32u + (unsigned)bit;
+            ++pos;
+        }
+    }
+}
+
+__global__ void qp3d_compact_kernel(const PlaneParams p) { compact_body(p, blockIdx.x); }
+
+// Fix-up of a speculative step.  If the true max lies in the window and the
+// list did not overflow, every listed cell (deferred and below the true
+// threshold) gets its S = 1 value: interior cells the stored one, PML cells
+// recomputed from the step's untouched inputs; otherwise *redo = 1 (set here
+// or by the resolution) and the gated exact re-run recomputes the whole step.
+__device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k, int *redo,
+                                           float *spec_err, unsigned block, unsigned nblocks)
+{
+    const unsigned n = *p.fix_count;
+    if (p.sres[1] == 0.0f) return;   // window missed: the step re-runs
+    if (n > p.alist_cap) {            // list overflow: re-run as well
+        if (block == 0 && threadIdx.x == 0) *redo = 1;
+        return;
+    }
+    (void)spec_err;
+    const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml, hy = ny - 2 * pml;
+    const unsigned plane = (unsigned)p.plane, ldy = (unsigned)p.ldy;
+    for (unsigned i = block * blockDim.x + threadIdx.x; i < n; i += nblocks * blockDim.x) {
+        const unsigned idx = p.alist[i];
+        const int z = (int)(idx / plane);
+        const unsigned rem = idx - (unsigned)z * plane;
+        const int x = (int)(rem / ldy), y = (int)(rem - (unsigned)x * ldy);
         const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
         const int fy = y < pml ? 2 : (y >= ny - pml ? 3 : -1);
         const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
         int f, li;
         cell_face(fx, x < pml ? pml - x : x - nx + pml, fy, y < pml ? pml - y : y - ny + pml, fz,
                   z < pml ? pml - z : z - nz + pml, f, li);
-        if (f < 0) {
-            const float Lp = fmaf(e2, __fadd_rn(Uxx, Uyy), Uzz);
-            out = fmaf(KS, Lp, fmaf(2.0f, u0, -p.u_prev[idx]));
+        float out;
+        if (f < 0) {   // interior cell: its S = 1 value was stored
+            out = p.av[idx];
         } else {
+            float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
+            cell_derivs(p.u_cur, idx, p.ldy, p.plane, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+            const float KS = __fmul_rn(p.prm_k[idx], 1.0f);
+            const float e2 = __fadd_rn(1.0f, p.prm_e[idx]);
             float n13, n21, n33, n3;
             out = pml_cell(f, p.layers[(f >> 1) * pml + li], KS, e2, Ux, Uy, Uz, Uxx, Uyy, Uzz,
                            p.dt, p.w1o[idx], p.w1c[idx], p.w21o[idx], p.w3o[idx], p.w3c[idx],
@@ -1136,8 +1224,12 @@ __device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k,
             p.pn[idx] = n3;
             p.w21n[idx] = n21;
             p.w3n[idx] = n33;
+            for (int e = 0; e < p.nsrc; ++e) {   // the step kernel's source add
+                const SrcEntry s = p.src[e];
+                if (s.x == x && s.y == y && s.z == z)
+                    out = __fadd_rn(out, __fmul_rn(s.v, p.wavelet));
+            }
         }
-        if (e.flags & 1u) out = __fadd_rn(out, e.v);
         p.u_out[idx] = out;
         if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
             p.record[(long long)(x - pml) * hy + (y - pml)] = out;
@@ -1273,9 +1365,15 @@ __global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, Pl
             p.win = b.win + 3 * (long long)k;
             p.spec_err = b.spec_err;
             p.delta_min = b.delta_min;
-            p.alt = b.alt;
+            p.spec_bias = b.spec_bias;
+            p.amask = b.amask;
+            p.am2 = b.am2;
+            p.av = b.av;
             p.alt_count = b.alt_count + k;
-            p.alt_cap = b.alt_cap;
+            p.alist = b.alist;
+            p.alist_cap = b.alist_cap;
+            p.fix_count = b.fix_count + k;
+            p.sres = b.sres + 2 * (long long)k;
         }
         pp[s] = p;
     }
@@ -1346,6 +1444,23 @@ __global__ void __launch_bounds__(kThreads, 2) qp3d_batch_plane_kernel(const __g
         }
         if (!ok) return;
     }
+}
+
+__global__ void qp3d_batch_resolve_kernel(const __grid_constant__ BatchArgs b, int nshots)
+{
+    for (int s = threadIdx.x; s < nshots; s += blockDim.x) {
+        const PlaneParams &p = b.pp[s];
+        if (p.active && p.spec)
+            resolve_body(p, const_cast<int *>(p.gate), const_cast<float *>(p.spec_err));
+    }
+}
+
+__global__ void qp3d_batch_compact_kernel(const __grid_constant__ BatchArgs b)
+{
+    const PlaneParams &p = b.pp[blockIdx.y];
+    if (!p.active || !p.spec) return;
+    if ((long long)blockIdx.x * blockDim.x * 4 >= defer_mask_words(p.plane * p.nz)) return;
+    compact_body(p, blockIdx.x);
 }
 
 __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
@@ -1428,6 +1543,12 @@ cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p
 cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
                          int nsm)
 {
+    const long long words = defer_mask_words(p.plane * p.nz);
+    qp3d_resolve_kernel<<<1, 32, 0, stream>>>(p, redo, spec_err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    qp3d_compact_kernel<<<(unsigned)((words / 4 + 255) / 256), 256, 0, stream>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     qp3d_fixup_kernel<<<8 * nsm, 256, 0, stream>>>(p, redo, spec_err);
     return cudaGetLastError();
 }
@@ -1462,8 +1583,14 @@ cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threa
 }
 
 cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,
-                               cudaStream_t stream)
+                               long long max_words, cudaStream_t stream)
 {
+    qp3d_batch_resolve_kernel<<<1, 128, 0, stream>>>(b, nshots);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    qp3d_batch_compact_kernel<<<dim3((unsigned)((max_words / 4 + 255) / 256), nshots), 256, 0,
+                                stream>>>(b);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     qp3d_batch_fixup_kernel<<<dim3(blocks_per_shot, nshots), 256, 0, stream>>>(b);
     return cudaGetLastError();
 }

@@ -483,6 +483,25 @@ static float mirror_gradmax(st32 *s, const mirror_coef *k)
     return gm;
 }
 
+/* 1/x as the kernels compute it: Newton-Raphson iterations r <- r + r(1 - x r)
+ * from the initial guess that negates the exponent of x in its integer
+ * representation (the device function rcp_nr, same constant and operation
+ * order, each step one fused multiply-add).  Within about 1 ulp of 1/x for
+ * normal positive x. */
+static inline float mirror_rcp(float x)
+{
+    uint32_t b;
+    float r;
+    memcpy(&b, &x, 4);
+    b = 0x7EF311C3u - b;
+    memcpy(&r, &b, 4);
+    for (int it = 0; it < 3; it++) {
+        float e = fmaf(-x, r, 1.0f);
+        r = fmaf(r, e, r);
+    }
+    return r;
+}
+
 /* Per-layer PML coefficients as the product derives them on the host. */
 typedef struct { float a1, a2, a3, dd; } layer_coef;
 
@@ -522,11 +541,11 @@ static void mirror_update(st32 *s, const oracle_args *a, const mirror_coef *k,
                 float m2 = fmaf(Uz, Uz, h2);
                 float S = 1.0f;
                 if (m2 > T2) {
-                    float aa = h2 / m2;
+                    float aa = h2 * mirror_rcp(m2);
                     float bb = 1.0f - aa;
                     float den = fmaf(e2x, aa, 1.0f);
                     float num = (r8 * aa) * bb;
-                    float q = num / (den * den);
+                    float q = num * mirror_rcp(den * den);
                     S = fmaf(0.5f, sqrtf(1.0f - q), 0.5f);
                 }
                 float KS = K * S;

@@ -21,12 +21,13 @@
  *                  (inputs promoted from float); used to state the FP32
  *                  rounding error of every result.
  *   ORACLE_MIRROR  FP32, the arithmetic the CUDA kernels perform (folded
- *                  1/dx coefficients, fused multiply-adds, IEEE division and
- *                  square root), written out operation by operation so that
- *                  a correct kernel matches it bit for bit.
+ *                  1/dx coefficients, fused multiply-adds, Newton-Raphson
+ *                  reciprocals in the scalar operator, IEEE square root),
+ *                  written out operation by operation so that a correct
+ *                  kernel matches it bit for bit.
  *
  * Parity pin: ORACLE_REF32 is checked bit-exact against the reference's own
- * CPU_function.c compiled from source (oracle/build_ref.sh); with that build
+ * CPU_function.c compiled from source (oracle/build.py); with that build
  * absent, the committed golden vectors under tests/golden/ pin it.
  *
  * Data layout: volumes are [nz][nx][ny] float, y fastest (array_new.c:2).

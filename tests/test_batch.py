@@ -62,7 +62,7 @@ def test_batch_matches_forward(shots, expected):
     dict(batch_tune=0, batch_candidate=4, batch_graph=0),
     dict(threshold_mode=0),
     dict(batch_mem_mb=1),
-    dict(alt_cap=1),
+    dict(spec_bias_ppm=500000),
     dict(spec_delta_ppm=0),
 ])
 def test_batch_settings(shots, expected, setting):
@@ -73,7 +73,7 @@ def test_batch_settings(shots, expected, setting):
         _same(recs, expected)
         if setting.get("batch_mem_mb"):
             assert st["groups"] == len(shots)
-        if setting.get("alt_cap"):
+        if setting.get("spec_bias_ppm"):
             assert st["redo_steps"] > 0
         if "batch_candidate" in setting:
             assert st["candidate"] == setting["batch_candidate"] and st["tuned"] == 0
