@@ -189,14 +189,14 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def traffic_per_cell():
-    """DRAM bytes per cell of one step-kernel launch from the committed ncu
-    summary (profiles/traffic.json), or None."""
+def traffic_ratio():
+    """DRAM bytes / algorithmic bytes of one step-kernel launch from the
+    committed ncu summary (profiles/traffic.json), or None."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
             d = json.load(f)
-        return float(d["qp3d_step_kernel"]["dram_bytes_per_cell"]), d["qp3d_step_kernel"].get("case")
+        return float(d["qp3d_step_kernel"]["traffic_over_algorithmic"]), d["qp3d_step_kernel"].get("case")
     except Exception:
         return None, None
 
@@ -314,21 +314,23 @@ def run_gpu_arm(args, dist):
     t_step = ms_step / n_launch / 1e3
     achieved = bstep / t_step / 1e9
     peak, peak_kind = hbm_peak()
-    tpc, tcase = traffic_per_cell()
+    tratio, tcase = traffic_ratio()
     roofline = {"bound": "hbm", "kernel": "qp3d_step_kernel", "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_kind": peak_kind + " copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
                 if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": bstep,
-                "traffic": (round(tpc * cells) if tpc else None),
-                "traffic_note": ("ncu dram read+write of one launch on %s, scaled per cell" % tcase)
-                if tpc else "no ncu capture committed",
+                "traffic": (round(tratio * bstep) if tratio else None),
+                "traffic_note": ("ncu dram read+write of one launch on %s, scaled to this grid by "
+                                 "its algorithmic bytes" % tcase) if tratio else
+                                "no ncu capture committed",
                 "step_kernel_ms": round(ms_step / n_launch, 5),
                 "threshold_overhead_ms": round(ms_grad / n_launch, 5),
                 "threshold_note": "per step: gradmax pre-pass for the first 3 steps, then the "
-                                  "fix-up kernel and the gated exact re-run of the speculative "
-                                  "step; last shot: %d re-runs in %d steps, max %d deferred "
-                                  "cells per step" % (int(redo.sum()), nt, int(alt.max()))}
+                                  "resolution, deferred-cell compaction and fix-up kernels and "
+                                  "the gated exact re-run of the speculative step; last shot: "
+                                  "%d re-runs in %d steps, max %d deferred cells per step" %
+                                  (int(redo.sum()), nt, int(alt.max()))}
 
     # end to end through the C ABI from pinned host memory
     pin = {}
