@@ -31,6 +31,11 @@ Nz0 in [128, 200], 20-cell PML, 10.8 M padded cells on average) cut from one
              (model upload, time loop, record download)
   single_shot_form  the same shots one qp3d call each: device time of the
              resident time loop and wall time of qp3d_forward
+
+--workload large measures the large mixed-precision configuration (one bench
+step = one shot): 800x800x400 cells + 40-cell PML (880x880x480 padded, 372 M
+cells), 20 dipping layers and 30 Gaussian velocity anomalies, 5000 steps,
+with vp/eps/delta stored as FP32 and as FP16 (param_fp16), wavefields FP32.
 """
 import argparse
 import json
@@ -68,7 +73,7 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="scale the horizontal/vertical extent (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="single", choices=["single", "batch"])
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "large"])
     ap.add_argument("--shots", type=int, default=64, help="batch workload: shots")
     return ap.parse_args()
 
@@ -90,7 +95,14 @@ def make_shot(w):
                                  seed=w["seed"])
 
 
-def algorithmic_bytes(shot):
+def algorithmic_bytes(shot, param_bytes=4):
+    """See below; param_bytes = bytes of each of vp, eps, delta per cell."""
+    b, ni, npml = _algorithmic_bytes(shot)
+    d = 3 * (4 - param_bytes)
+    return b - d * shot.N, ni, npml
+
+
+def _algorithmic_bytes(shot):
     """24 B per interior cell (read u(k), u(k-1), vp, eps, delta; write u(k+1))
     + 64 B per PML cell (u(k), vp, eps, delta, 7 state reads, 4 state writes,
     u(k+1)), over the updated box as the reference defines the layers."""
@@ -484,6 +496,67 @@ def run_batch_arm(args, dist):
     return 0
 
 
+LARGE_NAME = ("anomalous layered VTI 800x800x400 + 40-cell PML (880x880x480 padded), 20 dipping "
+              "layers + 30 Gaussian vp anomalies (+-15%%, sigma 10-40 cells) seed 5, %d steps x "
+              "0.5 ms, 20 Hz Ricker at surface centre, full-surface receivers")
+
+
+def run_large_arm(args, dist):
+    import qp3d
+    import synthetic
+    nt = args.nt if args.nt is not None else 5000
+    shot = synthetic.large_vti(nt=nt)
+    cells = shot.N
+    ctx = qp3d.Context(dist.local)
+    gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
+                 if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
+    peak, peak_kind = hbm_peak()
+    runs = {}
+    launches0 = ctx.launch_count()
+    clocks = Clocks(gpu_index)
+    for name, fp16 in (("fp32_params", 0), ("fp16_params", 1)):
+        ctx.tune(param_fp16=fp16)
+        ctx.load(shot)
+        for _ in range(args.warmup):
+            ctx.reset()
+            ctx.advance(nt)
+        ctx.sync()
+        tot = ms_s = 0.0
+        for _ in range(args.steps):
+            ctx.reset()
+            t, s, _ = ctx.time(nt)
+            tot += t
+            ms_s += s
+        bstep = algorithmic_bytes(shot, 2 if fp16 else 4)[0]
+        t_step = ms_s / (nt * args.steps) / 1e3
+        runs[name] = {"value": round(cells * nt * args.steps / (tot / 1e3) / 1e9, 3),
+                      "ms_per_step": round(tot / args.steps, 2),
+                      "step_kernel_ms": round(ms_s / (nt * args.steps), 5),
+                      "roofline": {"bound": "hbm", "achieved": round(bstep / t_step / 1e9, 1),
+                                   "peak": peak, "unit": "GB/s",
+                                   "frac": round(bstep / t_step / 1e9 / peak, 4),
+                                   "algorithmic_bytes_per_launch": bstep}}
+    clk = clocks.stop()
+    gpu_launches = ctx.launch_count() - launches0
+    if dist.rank == 0:
+        line = {
+            "metric": "Gcell-updates/s", "value": runs["fp16_params"]["value"], "unit": "Gcell/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": runs["fp16_params"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (params f16)",
+            "data": "synthetic",
+            "config": {"workload": LARGE_NAME % nt, "step": "one shot of %d time steps" % nt,
+                       "grid": [shot.nx, shot.ny, shot.nz], "cells": cells, "nt": nt,
+                       "l2": "inputs larger than L2", "parallelism": "single"},
+            "runs": runs,
+            "gpu_launches": gpu_launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -492,6 +565,8 @@ def main():
             return run_reference_arm(args, dist)
         if args.workload == "batch":
             return run_batch_arm(args, dist)
+        if args.workload == "large":
+            return run_large_arm(args, dist)
         return run_gpu_arm(args, dist)
     finally:
         dist.close()

@@ -61,6 +61,11 @@ static void free_shot(qp3d_ctx *ctx)
     ctx->amask = nullptr;
     ctx->alist = nullptr;
     ctx->alist_cap = 0;
+    __half **halves[] = {&ctx->h_vp, &ctx->h_eps, &ctx->h_del};
+    for (__half **h : halves) {
+        if (*h) cudaFree(*h);
+        *h = nullptr;
+    }
     if (ctx->layers) cudaFree(ctx->layers);
     if (ctx->src_fused) cudaFree(ctx->src_fused);
     if (ctx->src_band) cudaFree(ctx->src_band);
@@ -215,8 +220,9 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
 
+    const bool half = ctx->param_fp16 != 0;
     bool same = ctx->loaded && ctx->g.nx == g->nx && ctx->g.ny == g->ny && ctx->g.nz == g->nz &&
-                ctx->g.nt == g->nt && ctx->g.pml == g->pml;
+                ctx->g.nt == g->nt && ctx->g.pml == g->pml && ctx->half_loaded == half;
     if (!same) free_shot(ctx);
     ctx->g = *g;
     ctx->ldy = (g->ny + 31) & ~31;
@@ -226,15 +232,21 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     ctx->hy = g->ny - 2 * g->pml;
 
     if (!same) {
-        float **vols[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->K,     &ctx->E2,
-                          &ctx->R8,    &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0],
-                          &ctx->W3[1], &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],
-                          &ctx->W21[0], &ctx->W21[1]};
-        for (float **v : vols)
-            if ((rc = alloc_vol(ctx, v))) {
+        float **vols[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->W1[0], &ctx->W1[1],
+                          &ctx->W1[2], &ctx->W3[0], &ctx->W3[1], &ctx->W3[2], &ctx->P[0],
+                          &ctx->P[1],  &ctx->P[2],  &ctx->W21[0], &ctx->W21[1],
+                          &ctx->K,     &ctx->E2,    &ctx->R8};
+        const int nvols = half ? 14 : 17;   // half storage: no FP32 parameter volumes
+        for (int v = 0; v < nvols; ++v)
+            if ((rc = alloc_vol(ctx, vols[v]))) {
                 free_shot(ctx);
                 return rc;
             }
+        if (half) {
+            __half **hs[] = {&ctx->h_vp, &ctx->h_eps, &ctx->h_del};
+            for (__half **h : hs) CK(cudaMalloc(h, (size_t)ctx->vol * sizeof(__half)));
+        }
+        ctx->half_loaded = half;
         size_t nrec = (size_t)std::max(g->nt, 1) * ctx->hx * ctx->hy;
         CK(cudaMalloc(&ctx->record, nrec * sizeof(float)));
         CK(cudaMalloc(&ctx->gmax, (size_t)std::max(g->nt, 1) * sizeof(float)));
@@ -257,12 +269,23 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         ctx->alist_cap = (unsigned)std::min<long long>(std::max(1ll << 16, ctx->vol / 4), 0x7fffffff);
         CK(cudaMalloc(&ctx->alist, (size_t)ctx->alist_cap * sizeof(unsigned)));
     }
-    // model -> per-cell parameters (K, E2, R8 hold vp, eps, delta first)
-    if ((rc = upload_vol(ctx, ctx->K, m->vp)) || (rc = upload_vol(ctx, ctx->E2, m->epsilon)) ||
-        (rc = upload_vol(ctx, ctx->R8, m->delta)))
-        return rc;
-    CKL(launch_params(nullptr, nullptr, nullptr, ctx->K, ctx->E2, ctx->R8, ctx->vol, g->dt,
-                     ctx->stream));
+    if (half) {
+        // vp, eps, delta rounded to IEEE half (the wavefield buffers serve as
+        // FP32 staging; the reset below zeroes them)
+        const float *src[3] = {m->vp, m->epsilon, m->delta};
+        __half *dst[3] = {ctx->h_vp, ctx->h_eps, ctx->h_del};
+        for (int i = 0; i < 3; ++i) {
+            if ((rc = upload_vol(ctx, ctx->U[i], src[i]))) return rc;
+            CKL(launch_to_half(ctx->U[i], dst[i], ctx->vol, ctx->stream));
+        }
+    } else {
+        // model -> per-cell parameters (K, E2, R8 hold vp, eps, delta first)
+        if ((rc = upload_vol(ctx, ctx->K, m->vp)) || (rc = upload_vol(ctx, ctx->E2, m->epsilon)) ||
+            (rc = upload_vol(ctx, ctx->R8, m->delta)))
+            return rc;
+        CKL(launch_params(nullptr, nullptr, nullptr, ctx->K, ctx->E2, ctx->R8, ctx->vol, g->dt,
+                          ctx->stream));
+    }
     // coefficient tables
     derive_coefs(m->c, m->c2, g->dx, g->dy, g->dz, &ctx->coefs);
     if (g->pml > 0) {
@@ -382,6 +405,8 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.u_prev = ctx->U[b];
     p.u_out = ctx->U[c];
     p.prm_k = ctx->K; p.prm_e = ctx->E2; p.prm_r = ctx->R8;
+    p.h_vp = ctx->h_vp; p.h_eps = ctx->h_eps; p.h_del = ctx->h_del;
+    p.half_params = ctx->half_loaded ? 1 : 0;
     const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
     p.w1o = ctx->W1[lo]; p.w1c = ctx->W1[lc]; p.w1n = ctx->W1[ln];
     p.w3o = ctx->W3[lo]; p.w3c = ctx->W3[lc]; p.w3n = ctx->W3[ln];
@@ -810,6 +835,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "batch_mem_mb") && value >= 0) ctx->batch_mem_mb = value;
     else if (!strcmp(key, "spec_bias_ppm") && value >= -500000 && value <= 1000000)
         ctx->spec_bias = value * 1e-6f;
+    else if (!strcmp(key, "param_fp16") && (value == 0 || value == 1)) ctx->param_fp16 = value;
     else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
     if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
         CK(cudaSetDevice(ctx->device));
@@ -831,6 +857,7 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "threshold_mode")) return ctx->threshold_mode;
     if (!strcmp(key, "spec_delta_ppm")) return (int)(ctx->delta_min * 1e6f + 0.5f);
     if (!strcmp(key, "spec_bias_ppm")) return (int)lrintf(ctx->spec_bias * 1e6f);
+    if (!strcmp(key, "param_fp16")) return ctx->param_fp16;
     if (!strcmp(key, "batch_graph")) return ctx->batch_graph;
     if (!strcmp(key, "batch_tune")) return ctx->batch_tune;
     if (!strcmp(key, "batch_candidate")) return ctx->batch_candidate;

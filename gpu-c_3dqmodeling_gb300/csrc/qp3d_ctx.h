@@ -39,6 +39,8 @@ struct qp3d_ctx {
     bool rec_fused = true;
     float *U[3] = {nullptr, nullptr, nullptr};
     float *K = nullptr, *E2 = nullptr, *R8 = nullptr;
+    __half *h_vp = nullptr, *h_eps = nullptr, *h_del = nullptr;   // param_fp16 storage
+    bool half_loaded = false;        // the loaded shot stores its parameters as half
     float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21[2] = {};
     float *record = nullptr;
     float *gmax = nullptr;
@@ -75,6 +77,7 @@ struct qp3d_ctx {
     int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
     float delta_min = 0.01f;         // smallest half-width of the predicted window
     float spec_bias = 0.0f;          // test hook: shifts the predicted window
+    int param_fp16 = 0;              // store vp, eps, delta as IEEE half (next load)
     long long launches = 0;          // kernels launched by this context
     // batched shots (qp3d_batch)
     qp3d::BatchState *batch = nullptr;

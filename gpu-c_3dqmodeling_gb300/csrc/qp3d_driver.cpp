@@ -104,20 +104,28 @@ void shot_source(const qp3d_parameters &P, ShotInputs &in)
                 nx, ny, nz, in.source.data(), in.wavelet.data());
 }
 
-int model_shot(qp3d_ctx *ctx, const qp3d_parameters &P, ShotInputs &in, const float *c,
-               const float *c2, int snapflag, const char *snap_prefix, float *record, char *err,
-               size_t errlen)
+// Geometry and model of one shot (receivers on the top of the window, as
+// 3dPureqPModeling1.0.c:267 passes sz = pml).
+void shot_geom_model(const qp3d_parameters &P, ShotInputs &in, const float *c, const float *c2,
+                     qp3d_geom &g, qp3d_model &m)
 {
-    qp3d_geom g;
     g.nx = P.hx + 2 * P.pml; g.ny = P.hy + 2 * P.pml; g.nz = P.Nz0 + 2 * P.pml;
     g.nt = P.nt; g.pml = P.pml; g.sz = P.pml;
     g.dx = P.dx; g.dy = P.dy; g.dz = P.dz; g.dt = P.dt;
-    qp3d_model m;
     m.vp = in.vp.data(); m.epsilon = in.eps.data(); m.delta = in.del.data();
     m.source = in.source.data(); m.wavelet = in.wavelet.data();
     m.dlr = in.prof[0].data(); m.ddlr = in.prof[1].data(); m.dtb = in.prof[2].data();
     m.ddtb = in.prof[3].data(); m.dfb = in.prof[4].data(); m.ddfb = in.prof[5].data();
     m.c = c; m.c2 = c2;
+}
+
+int model_shot(qp3d_ctx *ctx, const qp3d_parameters &P, ShotInputs &in, const float *c,
+               const float *c2, int snapflag, const char *snap_prefix, float *record, char *err,
+               size_t errlen)
+{
+    qp3d_geom g;
+    qp3d_model m;
+    shot_geom_model(P, in, c, c2, g, m);
     std::string prefix(snap_prefix);
     qp3d_snap snap;
     snap.ntsnap = P.ntsnap;
@@ -175,7 +183,7 @@ extern "C" int qp3d_parse_parameter_file(const char *path, qp3d_parameters *P, c
 extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options *opt, char *err,
                                        size_t errlen)
 {
-    qp3d_run_options o{0, QP3D_DIRECT_SOURCE_CELL, 0.f, 0.f, 0.f, 0};
+    qp3d_run_options o{0, QP3D_DIRECT_SOURCE_CELL, 0.f, 0.f, 0.f, 0, 0};
     if (opt) o = *opt;
     qp3d_parameters P;
     int rc = qp3d_parse_parameter_file(path, &P, err, errlen);
@@ -188,7 +196,7 @@ extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options 
     qp3d_ctx *ctx = nullptr;
     rc = qp3d_ctx_create(o.device, &ctx);
     if (rc) return fail(err, errlen, rc, "no CUDA device %d", o.device);
-    std::vector<float> rec_full(nrec), rec_direct(nrec, 0.0f), rec_mute(nrec);
+    std::vector<float> rec_direct(nrec, 0.0f), rec_mute(nrec);
     ShotInputs in;
 
     // direct wave (Main.c:148-160), once before the shot loop
@@ -214,41 +222,73 @@ extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options 
             goto done;
         }
     }
-    // shot loop (Main.c:162-246): x slow, y fast
-    for (int ix = 0; ix < P.nxshot; ++ix)
-        for (int iy = 0; iy < P.nyshot; ++iy) {
-            const int sx = P.sx0 + ix * P.dxshot, sy = P.sy0 + iy * P.dyshot;
-            if (o.verbose) printf("shot %d at (%d,%d)\n", ix * P.nyshot + iy, sx, sy);
-            if ((rc = read_shot_model(P, sx, sy, in, err, errlen))) goto done;
-            shot_source(P, in);
-            if ((rc = model_shot(ctx, P, in, c, c2, P.snapflag_full, P.snap_full, rec_full.data(),
-                                 err, errlen)))
-                goto done;
-            for (size_t i = 0; i < nrec; ++i) rec_mute[i] = rec_full[i] - rec_direct[i];
-            if (write_file(P.recfull_file, rec_full.data(), nrec, "ab") ||
-                write_file(P.recmut_file, rec_mute.data(), nrec, "ab")) {
-                rc = fail(err, errlen, QP3D_ERR_IO, "cannot append %s / %s", P.recfull_file,
-                          P.recmut_file);
+    // shot loop (Main.c:162-246): x slow, y fast.  Without per-shot
+    // snapshots the shots go through qp3d_batch in groups that fit the host
+    // memory budget; the output files are written in the same order.
+    {
+        std::vector<std::pair<int, int>> pos;
+        for (int ix = 0; ix < P.nxshot; ++ix)
+            for (int iy = 0; iy < P.nyshot; ++iy)
+                pos.push_back({P.sx0 + ix * P.dxshot, P.sy0 + iy * P.dyshot});
+        const bool batched = !(P.snapflag_full == 1 && P.ntsnap > 0) && o.shots_per_call != 1;
+        const size_t per_shot = (4 * n + nrec + (size_t)P.nt) * sizeof(float);
+        size_t group = 1;
+        if (batched)
+            group = o.shots_per_call > 1 ? (size_t)o.shots_per_call
+                                         : std::max<size_t>(1, (16ull << 30) / per_shot);
+        for (size_t g0 = 0; g0 < pos.size(); g0 += group) {
+            const size_t cnt = std::min(group, pos.size() - g0);
+            std::vector<ShotInputs> ins(cnt);
+            std::vector<std::vector<float>> recs(cnt, std::vector<float>(nrec));
+            for (size_t i = 0; i < cnt; ++i) {
+                const int sx = pos[g0 + i].first, sy = pos[g0 + i].second;
+                if (o.verbose) printf("shot %zu at (%d,%d)\n", g0 + i, sx, sy);
+                if ((rc = read_shot_model(P, sx, sy, ins[i], err, errlen))) goto done;
+                shot_source(P, ins[i]);
+            }
+            if (batched) {
+                std::vector<qp3d_shot> shots(cnt);
+                for (size_t i = 0; i < cnt; ++i) {
+                    shot_geom_model(P, ins[i], c, c2, shots[i].geom, shots[i].model);
+                    shots[i].record = recs[i].data();
+                }
+                if ((rc = qp3d_batch(ctx, (int)cnt, shots.data()))) {
+                    rc = fail(err, errlen, rc, "modeling failed: %s", qp3d_ctx_last_error(ctx));
+                    goto done;
+                }
+            } else if ((rc = model_shot(ctx, P, ins[0], c, c2, P.snapflag_full, P.snap_full,
+                                        recs[0].data(), err, errlen))) {
                 goto done;
             }
-            if (ix == 0 && iy == 0) {
-                // the reference writes the muted slices, then overwrites the
-                // same files with the full-wave slices (Main.c:216-245)
-                const int jy = (P.hy - 1) / 2, ixs = (P.hx - 1) / 2;
-                std::vector<float> xz((size_t)P.nt * P.hx), yz((size_t)P.nt * P.hy);
-                for (int k = 0; k < P.nt; ++k) {
-                    for (int i = 0; i < P.hx; ++i)
-                        xz[(size_t)k * P.hx + i] = rec_full[((size_t)k * P.hx + i) * P.hy + jy];
-                    for (int j = 0; j < P.hy; ++j)
-                        yz[(size_t)k * P.hy + j] = rec_full[((size_t)k * P.hx + ixs) * P.hy + j];
-                }
-                if (write_file(P.recxz_file, xz.data(), xz.size(), "wb") ||
-                    write_file(P.recyz_file, yz.data(), yz.size(), "wb")) {
-                    rc = fail(err, errlen, QP3D_ERR_IO, "cannot write the record slices");
+            for (size_t i = 0; i < cnt; ++i) {
+                const std::vector<float> &rec_full = recs[i];
+                for (size_t j = 0; j < nrec; ++j) rec_mute[j] = rec_full[j] - rec_direct[j];
+                if (write_file(P.recfull_file, rec_full.data(), nrec, "ab") ||
+                    write_file(P.recmut_file, rec_mute.data(), nrec, "ab")) {
+                    rc = fail(err, errlen, QP3D_ERR_IO, "cannot append %s / %s", P.recfull_file,
+                              P.recmut_file);
                     goto done;
+                }
+                if (g0 + i == 0) {
+                    // the reference writes the muted slices, then overwrites
+                    // the same files with the full-wave slices (Main.c:216-245)
+                    const int jy = (P.hy - 1) / 2, ixs = (P.hx - 1) / 2;
+                    std::vector<float> xz((size_t)P.nt * P.hx), yz((size_t)P.nt * P.hy);
+                    for (int k = 0; k < P.nt; ++k) {
+                        for (int x = 0; x < P.hx; ++x)
+                            xz[(size_t)k * P.hx + x] = rec_full[((size_t)k * P.hx + x) * P.hy + jy];
+                        for (int y = 0; y < P.hy; ++y)
+                            yz[(size_t)k * P.hy + y] = rec_full[((size_t)k * P.hx + ixs) * P.hy + y];
+                    }
+                    if (write_file(P.recxz_file, xz.data(), xz.size(), "wb") ||
+                        write_file(P.recyz_file, yz.data(), yz.size(), "wb")) {
+                        rc = fail(err, errlen, QP3D_ERR_IO, "cannot write the record slices");
+                        goto done;
+                    }
                 }
             }
         }
+    }
 done:
     qp3d_ctx_destroy(ctx);
     return rc;

@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -77,6 +78,10 @@ struct PlaneParams {
     const float *u_prev;
     float *u_out;
     const float *prm_k, *prm_e, *prm_r;
+    // half-precision parameter storage (half_params != 0): vp, eps, delta as
+    // IEEE half, widened in the kernels; prm_* are unused then
+    const __half *h_vp, *h_eps, *h_del;
+    int half_params;
     const float *w1o, *w1c; float *w1n;   // w11, w12 -> w13
     const float *w3o, *w3c; float *w3n;   // w31, w32 -> w33
     const float *po, *pc; float *pn;      // p1, p2 -> p3
@@ -185,6 +190,8 @@ cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0,
 cudaError_t launch_params(const float *vp, const float *eps, const float *del,
                           float *K, float *E2, float *R8, long long n, float dt,
                           cudaStream_t stream);
+// vp, eps, delta (pitched FP32) -> IEEE half, round to nearest even
+cudaError_t launch_to_half(const float *a, __half *h, long long n, cudaStream_t stream);
 // Dynamic shared memory of a plane kernel; nsrc = fused sources of the shot
 // (the per-CTA source list has room for all of them).
 size_t plane_smem_bytes(int tile_x, int pml, int nsrc = kMaxFusedSources);

@@ -815,7 +815,46 @@ __device__ __forceinline__ float aniso_s(float h2, float m2, float e2x, float r8
 // One tile column [z0, z1) of the step.  The grid kernel below runs one per
 // CTA; the batched kernel runs many per CTA (REUSE: barriers invalidated at
 // the end, return value uniform over the CTA; false = a wait timed out).
-template <bool SPEC, bool REUSE>
+// Per-cell parameters of a quad from half-precision vp, eps, delta, with the
+// operations of qp3d_params_kernel: (vp dt)^2, 2 eps, 8 (eps - delta).
+__device__ __forceinline__ void quad_params_half(const PlaneParams &p, uint2 hv, uint2 he,
+                                                 uint2 hd, float4 &K, float4 &E2, float4 &R8)
+{
+    const float2 v0 = __half22float2(*reinterpret_cast<const __half2 *>(&hv.x));
+    const float2 v1 = __half22float2(*reinterpret_cast<const __half2 *>(&hv.y));
+    const float2 e0 = __half22float2(*reinterpret_cast<const __half2 *>(&he.x));
+    const float2 e1 = __half22float2(*reinterpret_cast<const __half2 *>(&he.y));
+    const float2 d0 = __half22float2(*reinterpret_cast<const __half2 *>(&hd.x));
+    const float2 d1 = __half22float2(*reinterpret_cast<const __half2 *>(&hd.y));
+    const float vp[4] = {v0.x, v0.y, v1.x, v1.y}, ep[4] = {e0.x, e0.y, e1.x, e1.y},
+                de[4] = {d0.x, d0.y, d1.x, d1.y};
+    float k[4], e[4], r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float vdt = __fmul_rn(vp[j], p.dt);
+        k[j] = __fmul_rn(vdt, vdt);
+        e[j] = __fmul_rn(2.0f, ep[j]);
+        r[j] = __fmul_rn(8.0f, __fsub_rn(ep[j], de[j]));
+    }
+    K = make_float4(k[0], k[1], k[2], k[3]);
+    E2 = make_float4(e[0], e[1], e[2], e[3]);
+    R8 = make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// (vp dt)^2 and 2 eps of one cell, from either storage
+__device__ __forceinline__ float cell_K(const PlaneParams &p, long long i)
+{
+    if (!p.half_params) return p.prm_k[i];
+    const float vdt = __fmul_rn(__half2float(p.h_vp[i]), p.dt);
+    return __fmul_rn(vdt, vdt);
+}
+
+__device__ __forceinline__ float cell_E2(const PlaneParams &p, long long i)
+{
+    return p.half_params ? __fmul_rn(2.0f, __half2float(p.h_eps[i])) : p.prm_e[i];
+}
+
+template <bool SPEC, bool REUSE, bool HALF = false>
 __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlaneParams &p,
                                           const Coefs &k, int tile_x, int y0, int x0, int z0,
                                           int z1, bool win_writer, unsigned char *smem)
@@ -898,11 +937,18 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         const int liz = z < pml ? pml - z : z - nz + pml;
         const bool pml_quad = xy_face || (row_ok && fz >= 0);
         float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
+        uint2 hv = make_uint2(0u, 0u), he = hv, hd = hv;
         if (row_ok) {
             u1v = ldg4(p.u_prev + base);
-            Kv = ldg4(p.prm_k + base);
-            Ev = ldg4(p.prm_e + base);
-            Rv = ldg4(p.prm_r + base);
+            if (HALF) {   // widened after the stencil, when the loads have landed
+                hv = __ldg(reinterpret_cast<const uint2 *>(p.h_vp + base));
+                he = __ldg(reinterpret_cast<const uint2 *>(p.h_eps + base));
+                hd = __ldg(reinterpret_cast<const uint2 *>(p.h_del + base));
+            } else {
+                Kv = ldg4(p.prm_k + base);
+                Ev = ldg4(p.prm_e + base);
+                Rv = ldg4(p.prm_r + base);
+            }
         }
         float4 w11 = zero4, w12 = zero4, w31 = zero4, w32 = zero4, p1 = zero4, p2 = zero4,
                w21 = zero4;
@@ -921,6 +967,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         if (!ok) break;
         float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
         quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        if (HALF) quad_params_half(p, hv, he, hd, Kv, Ev, Rv);
         // scalar operator, GPU_kernel.cu:93-111
         float h2[4], m2[4];
         bool above[4], amb[4];
@@ -1045,7 +1092,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
     return ok;
 }
 
-template <bool SPEC>
+template <bool SPEC, bool HALF>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
@@ -1055,8 +1102,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int z0 = kRadius + blockIdx.z * p.chunk_z;
     const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
     if (z0 >= z1) return;
-    step_tile<SPEC, false>(&tm_u, p, p.k, p.tile_x, y0, x0, z0, z1,
-                           blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
+    step_tile<SPEC, false, HALF>(&tm_u, p, p.k, p.tile_x, y0, x0, z0, z1,
+                                 blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
 }
 
 // Derivatives of u at one cell from global memory, in the same operation
@@ -1214,8 +1261,8 @@ __device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k,
         } else {
             float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
             cell_derivs(p.u_cur, idx, p.ldy, p.plane, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
-            const float KS = __fmul_rn(p.prm_k[idx], 1.0f);
-            const float e2 = __fadd_rn(1.0f, p.prm_e[idx]);
+            const float KS = __fmul_rn(cell_K(p, idx), 1.0f);
+            const float e2 = __fadd_rn(1.0f, cell_E2(p, idx));
             float n13, n21, n33, n3;
             out = pml_cell(f, p.layers[(f >> 1) * pml + li], KS, e2, Ux, Uy, Uz, Uxx, Uyy, Uzz,
                            p.dt, p.w1o[idx], p.w1c[idx], p.w21o[idx], p.w3o[idx], p.w3c[idx],
@@ -1471,6 +1518,13 @@ __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
                gridDim.x);
 }
 
+__global__ void qp3d_to_half_kernel(const float *a, __half *h, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        h[i] = __float2half_rn(a[i]);
+}
+
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
@@ -1487,10 +1541,13 @@ cudaError_t configure_kernels()
     if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<2>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
-    if ((e = cudaFuncSetAttribute(qp3d_step_kernel<true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    if ((e = cudaFuncSetAttribute(qp3d_step_kernel<false>,
+    if ((e = cudaFuncSetAttribute(qp3d_step_kernel<true, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
+        (e = cudaFuncSetAttribute(qp3d_step_kernel<false, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
+        (e = cudaFuncSetAttribute(qp3d_step_kernel<true, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
+        (e = cudaFuncSetAttribute(qp3d_step_kernel<false, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
         return e;
     if ((e = cudaFuncSetAttribute(qp3d_gradmax_kernel<true>,
@@ -1516,10 +1573,14 @@ cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 g
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
                         cudaStream_t stream)
 {
-    if (p.spec)
-        qp3d_step_kernel<true><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
-    else
-        qp3d_step_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+    const int t = plane_threads(p.tile_x);
+    if (p.half_params) {
+        if (p.spec) qp3d_step_kernel<true, true><<<grid, t, smem, stream>>>(tm_u, p);
+        else qp3d_step_kernel<false, true><<<grid, t, smem, stream>>>(tm_u, p);
+    } else {
+        if (p.spec) qp3d_step_kernel<true, false><<<grid, t, smem, stream>>>(tm_u, p);
+        else qp3d_step_kernel<false, false><<<grid, t, smem, stream>>>(tm_u, p);
+    }
     return cudaGetLastError();
 }
 
@@ -1633,6 +1694,13 @@ cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0, int 
     long long b = (n + 255) / 256;
     int blocks = (int)(b > 8192 ? 8192 : b);
     qp3d_crop_kernel<<<blocks, 256, 0, stream>>>(u, out, x0, x1, y0, y1, z0, z1, ldy, plane);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_half(const float *a, __half *h, long long n, cudaStream_t stream)
+{
+    long long b = (n + 255) / 256;
+    qp3d_to_half_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(a, h, n);
     return cudaGetLastError();
 }
 

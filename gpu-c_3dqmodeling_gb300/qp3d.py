@@ -88,7 +88,8 @@ DIRECT_SOURCE_CELL, DIRECT_ZERO, DIRECT_VALUES = 0, 1, 2
 class RunOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("direct_model", ctypes.c_int),
                 ("direct_vp", ctypes.c_float), ("direct_eps", ctypes.c_float),
-                ("direct_del", ctypes.c_float), ("verbose", ctypes.c_int)]
+                ("direct_del", ctypes.c_float), ("verbose", ctypes.c_int),
+                ("shots_per_call", ctypes.c_int)]
 
 
 # every symbol include/qp3d.h and include/qp3d_driver.h declare
@@ -232,9 +233,10 @@ def parse_parameter_file(path):
 
 
 def run_parameter_file(path, device=0, direct_model=DIRECT_SOURCE_CELL, direct=(0.0, 0.0, 0.0),
-                       verbose=False):
+                       verbose=False, shots_per_call=0):
     """qp3d_run_parameter_file -> (rc, message)."""
-    o = RunOptions(device, direct_model, direct[0], direct[1], direct[2], int(verbose))
+    o = RunOptions(device, direct_model, direct[0], direct[1], direct[2], int(verbose),
+                   int(shots_per_call))
     err = ctypes.create_string_buffer(512)
     rc = load().qp3d_run_parameter_file(str(path).encode(), ctypes.byref(o), err, len(err))
     return rc, err.value.decode()

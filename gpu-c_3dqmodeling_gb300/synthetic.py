@@ -76,6 +76,43 @@ def layered_vti(hx=400, hy=400, nz0=300, pml=30, nt=3000, dx=10.0, dt=5e-4, fm=2
     return _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=src)
 
 
+def anomalous_volume(hx=800, hy=800, nz0=400, nlayers=20, nanom=30, seed=5, slope=0.15,
+                     sigma=(10.0, 40.0), amp=0.15):
+    """Interior vp, eps, delta of the large workload: layered_volume with
+    nlayers layers plus nanom Gaussian velocity anomalies (relative amplitude
+    uniform in [-amp, amp], sigma uniform in the given range of cells, centres
+    uniform in the volume), each evaluated within 3 sigma of its centre."""
+    vp, eps, de = layered_volume(hx, hy, nz0, nlayers, seed, slope)
+    rng = np.random.default_rng(seed + 2000)
+    scale = np.ones((nz0, hx, hy), np.float32)
+    for _ in range(nanom):
+        cz, cx, cy = rng.uniform(0, nz0), rng.uniform(0, hx), rng.uniform(0, hy)
+        s = rng.uniform(*sigma)
+        a = rng.uniform(-amp, amp)
+        lo = [max(0, int(c - 3 * s)) for c in (cz, cx, cy)]
+        hi = [min(n, int(c + 3 * s) + 1) for c, n in zip((cz, cx, cy), (nz0, hx, hy))]
+        if any(h <= l for l, h in zip(lo, hi)):
+            continue
+        z = (np.arange(lo[0], hi[0]) - cz)[:, None, None]
+        x = (np.arange(lo[1], hi[1]) - cx)[None, :, None]
+        y = (np.arange(lo[2], hi[2]) - cy)[None, None, :]
+        g = np.exp(-(z * z + x * x + y * y) / (2.0 * s * s)).astype(np.float32)
+        scale[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] += np.float32(a) * g
+    return (vp * scale).astype(np.float32), eps, de
+
+
+def large_vti(hx=800, hy=800, nz0=400, pml=40, nt=5000, dx=10.0, dt=5e-4, fm=20.0, seed=5,
+              decimate=1):
+    """Large workload: anomalous_volume, 40-cell PML, 5000 steps.  decimate=k
+    keeps every k-th cell of the full-size model (spacing k*dx) for the
+    oracle comparisons."""
+    vp, eps, de = anomalous_volume(hx, hy, nz0, seed=seed)
+    if decimate > 1:
+        k = decimate
+        vp, eps, de = (np.ascontiguousarray(a[::k, ::k, ::k]) for a in (vp, eps, de))
+    return _finish(vp, eps, de, pml, dx * decimate, dt, nt, fm)
+
+
 def batch_windows(nshots=64, seed=3, model=(512, 512, 200), hrange=(128, 256),
                   zrange=(128, 200), frange=(15.0, 30.0)):
     """Apertures of the batched workload: per shot (x0, y0, hx, hy, nz0, fm)

@@ -190,8 +190,11 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * "batch_graph" (1: replay steps from a captured graph), "batch_tune"
  * (1: time the candidate shapes), "batch_candidate" (shape index used when
  * not tuning, -1 = default), "batch_mem_mb" (device memory for one group of
- * resident shots, 0 = what is free).  All settings compute identical
- * results. */
+ * resident shots, 0 = what is free).  All these settings compute identical
+ * results.  "param_fp16" (1: the next qp3d_shot_load / qp3d_forward stores
+ * vp, epsilon and delta as IEEE half, rounded to nearest; the stencil stays
+ * FP32, and the results equal an FP32 run on the rounded model bit for bit;
+ * qp3d_batch always stores FP32). */
 int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
 int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
 

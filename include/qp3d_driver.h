@@ -49,6 +49,11 @@ typedef struct {
     int direct_model;              /* QP3D_DIRECT_* */
     float direct_vp, direct_eps, direct_del;
     int verbose;                   /* progress lines on stdout */
+    int shots_per_call;            /* 0: shots go through qp3d_batch in groups that
+                                      fit 16 GB of host memory (one by one when
+                                      full-wave snapshots are requested);
+                                      1: one qp3d_forward per shot, as the
+                                      reference; N > 1: at most N per call */
 } qp3d_run_options;
 
 /* Parse a parameter file.  Returns QP3D_OK, QP3D_ERR_IO (cannot open) or
@@ -58,7 +63,8 @@ int qp3d_parse_parameter_file(const char *path, qp3d_parameters *out, char *err,
 /* Run the whole modeling job a parameter file describes, writing the same
  * files as the reference program: Record_fullwave and Record_mute appended
  * shot after shot (read_write.c:66-77), Record_direct, the first shot's xz/yz
- * record slices, and snapshots through modeling3d's naming.  Unlike the
+ * record slices, and snapshots through modeling3d's naming.  The records do
+ * not depend on shots_per_call.  Unlike the
  * reference it stops with an error when a model window leaves the model or a
  * file cannot be read or written.  opt may be NULL (defaults). */
 int qp3d_run_parameter_file(const char *path, const qp3d_run_options *opt, char *err,

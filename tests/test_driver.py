@@ -42,16 +42,22 @@ def test_parse_errors(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("direct", ["values", "source"])
-def test_modeling_job_matches_oracle(tmp_path, direct):
+@pytest.mark.parametrize("direct,snapfull,per_call,nxshot", [
+    ("values", 1, 0, 1),     # full-wave snapshots: one qp3d_forward per shot
+    ("source", 1, 0, 1),
+    ("values", 0, 0, 2),     # no snapshots: all four shots in one qp3d_batch call
+    ("values", 0, 3, 2),     # groups of three and one
+    ("values", 0, 1, 2),     # one shot per call, as the reference
+])
+def test_modeling_job_matches_oracle(tmp_path, direct, snapfull, per_call, nxshot):
     d = str(tmp_path)
-    path, c, models = write_case(d)
+    path, c, models = write_case(d, snapfull=snapfull, nxshot=nxshot)
     if direct == "values":
         rc, msg = qp3d.run_parameter_file(path, direct_model=qp3d.DIRECT_VALUES,
-                                          direct=(2100.0, 0.1, 0.05))
+                                          direct=(2100.0, 0.1, 0.05), shots_per_call=per_call)
         dvals = (2100.0, 0.1, 0.05)
     else:
-        rc, msg = qp3d.run_parameter_file(path)
+        rc, msg = qp3d.run_parameter_file(path, shots_per_call=per_call)
         fny, fnx = c["sy0"] - (c["hy"] - 1) // 2, c["sx0"] - (c["hx"] - 1) // 2
         cell = (fny + (c["hy"] - 1) // 2, fnx + (c["hx"] - 1) // 2, 0)
         dvals = tuple(float(m[cell]) for m in models)
@@ -77,6 +83,9 @@ def test_modeling_job_matches_oracle(tmp_path, direct):
             yz = np.fromfile(os.path.join(d, "recordyz.dat"), np.float32).reshape(nt, hy)
             assert bits_equal(xz, rec[:, :, (hy - 1) // 2])
             assert bits_equal(yz, rec[:, (hx - 1) // 2, :])
+    if not snapfull:
+        assert not os.path.exists(os.path.join(d, "snapshot_fullwave0.dat"))
+        return
     # snapshots of the last shot (each shot overwrites the same names)
     pml, Nz0 = c["pml"], c["Nz0"]
     st = None

@@ -1,0 +1,60 @@
+"""Half-precision parameter storage (param_fp16): vp, epsilon and delta kept
+as IEEE half in HBM, stencil and wavefields in FP32.
+
+The kernels widen the halves and derive (vp dt)^2, 2 eps, 8 (eps - delta)
+with the operations of the FP32 path, so a half-storage run equals an FP32
+run on the half-rounded model bit for bit; the rounding itself is measured
+against the FP64 oracle beside the FP32 run's error.
+"""
+import numpy as np
+import pytest
+
+import qp3d
+import synthetic
+from helpers import bits_equal, rel_l2
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _rounded(shot):
+    r = lambda a: a.astype(np.float16).astype(np.float32)
+    return qp3d.Shot(shot.nx, shot.ny, shot.nz, shot.pml, shot.sz, shot.dx, shot.dy, shot.dz,
+                     shot.dt, r(shot.vp), r(shot.eps), r(shot.delta), shot.src, shot.wavelet,
+                     shot.prof, shot.c, shot.c2)
+
+
+def _run(shot, fp16, **tune):
+    with qp3d.Context(0) as ctx:
+        ctx.tune(param_fp16=fp16, **tune)
+        rec = ctx.forward(shot)
+        ctx.load(shot)
+        ctx.advance(shot.nt)
+        return rec, ctx.record(), ctx.uxyzmax()
+
+
+@pytest.mark.parametrize("threshold_mode", [1, 0])
+def test_half_storage_equals_fp32_on_rounded_model(threshold_mode):
+    shot = synthetic.small_case(hx=26, hy=22, nz0=20, pml=8, nt=70, seed=31)
+    rec_h, rec_h2, mx_h = _run(shot, 1, threshold_mode=threshold_mode)
+    rec_r, _, mx_r = _run(_rounded(shot), 0, threshold_mode=threshold_mode)
+    assert bits_equal(rec_h, rec_r)
+    assert bits_equal(rec_h2, rec_r)       # staged form too
+    assert bits_equal(mx_h, mx_r)
+    rec_f, _, _ = _run(shot, 0)
+    assert not bits_equal(rec_h, rec_f)    # the rounding did happen
+
+
+def test_half_storage_error_against_fp64():
+    """Decimated copy of the large workload (every 8th cell: 100x100x50
+    interior at 80 m, 20-cell PML), 400 steps."""
+    shot = synthetic.large_vti(pml=20, nt=400, decimate=8, fm=8.0)
+    rec_h, _, _ = _run(shot, 1)
+    rec_f, _, _ = _run(shot, 0)
+    r64, _, _ = O.run(O.F64, shot.to_oracle(O))
+    e_h, e_f = rel_l2(rec_h, r64), rel_l2(rec_f, r64)
+    print("large workload / 8: record rel-L2 vs FP64: FP16 params %.3e, FP32 params %.3e"
+          % (e_h, e_f))
+    assert e_f < 1e-4
+    assert e_h < 5e-2
+    assert e_h > e_f
