@@ -31,11 +31,11 @@ def _newer(target, sources):
 
 
 def build_oracle(force=False):
-    src = os.path.join(HERE, "qp3d_oracle.c")
+    srcs = [os.path.join(HERE, "qp3d_oracle.c"), os.path.join(HERE, "qp3d_adjoint.c")]
     hdr = os.path.join(HERE, "qp3d_oracle.h")
-    if force or _newer(LIB, [src, hdr]):
+    if force or _newer(LIB, srcs + [hdr]):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
-        cmd = ["gcc", "-std=c11", "-Wall"] + COMMON + ["-o", LIB, src, "-lm"]
+        cmd = ["gcc", "-std=c11", "-Wall"] + COMMON + ["-o", LIB] + srcs + ["-lm"]
         subprocess.check_call(cmd)
     return LIB
 

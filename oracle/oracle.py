@@ -231,3 +231,103 @@ def run_reference(prob, k0=0, nsteps=None, state=None):
     if rc != 0:
         raise RuntimeError("ref_run failed: %d" % rc)
     return rec, mx, state
+
+
+# ---------------------------------------------------------------------------
+# FP64 adjoint (qp3d_adjoint.c)
+# ---------------------------------------------------------------------------
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+class AdjArgs(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("pml", ctypes.c_int), ("sz", ctypes.c_int), ("nt", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("vp", _f64p), ("eps", _f64p), ("del_", _f64p),
+        ("source", _f32p), ("wavelet", _f32p),
+        ("dlr", _f32p), ("ddlr", _f32p), ("dtb", _f32p), ("ddtb", _f32p),
+        ("dfb", _f32p), ("ddfb", _f32p),
+        ("c", _f32p), ("c2", _f32p),
+        ("nthreads", ctypes.c_int),
+    ]
+
+
+def _adj_lib():
+    L = lib()
+    if not getattr(L, "_adj_ready", False):
+        P = ctypes.POINTER(AdjArgs)
+        L.oracle_adj_freeze.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_adj_forward.argtypes = [P] + [ctypes.c_void_p] * 5
+        L.oracle_adj_backward.argtypes = [P] + [ctypes.c_void_p] * 8
+        for f in (L.oracle_adj_freeze, L.oracle_adj_forward, L.oracle_adj_backward):
+            f.restype = ctypes.c_int
+        L._adj_ready = True
+    return L
+
+
+class Adjoint:
+    """FP64 frozen-operator forward and adjoint of one problem.  The model is
+    held in double (vp, eps, delta as float64 arrays of N cells) so finite
+    differences can perturb it; the scalar operator is frozen by freeze()."""
+
+    def __init__(self, prob, source=True, nthreads=0):
+        self.p = prob
+        self.vp = prob.vp.astype(np.float64)
+        self.eps = prob.eps.astype(np.float64)
+        self.delta = prob.delta.astype(np.float64)
+        self.use_source = source
+        self.nthreads = nthreads
+        self.fa = self.fb = None
+
+    def _args(self, vp=None, eps=None, delta=None):
+        p = self.p
+        self._keep = [np.ascontiguousarray(v if v is not None else d, np.float64)
+                      for v, d in ((vp, self.vp), (eps, self.eps), (delta, self.delta))]
+        a = AdjArgs()
+        a.nx, a.ny, a.nz, a.pml, a.sz, a.nt = p.nx, p.ny, p.nz, p.pml, p.sz, p.nt
+        a.dx, a.dy, a.dz, a.dt = p.dx, p.dy, p.dz, p.dt
+        a.vp, a.eps, a.del_ = [k.ctypes.data_as(_f64p) for k in self._keep]
+        a.source = _fp(p.src) if (self.use_source and p.src is not None) else None
+        a.wavelet = _fp(p.wavelet)
+        a.dlr, a.ddlr, a.dtb, a.ddtb, a.dfb, a.ddfb = [_fp(x) for x in p.prof]
+        a.c, a.c2 = _fp(p.c), _fp(p.c2)
+        a.nthreads = self.nthreads
+        return a
+
+    def freeze(self, with_source=True):
+        """Frozen factors from a base run (the live operator), by default with
+        the problem's source even when the adjoint runs without it."""
+        n = self.p.N * self.p.nt
+        self.fa = np.zeros(n, np.float64)
+        self.fb = np.zeros(n, np.float64)
+        keep, self.use_source = self.use_source, with_source
+        a = self._args()
+        self.use_source = keep
+        rc = _adj_lib().oracle_adj_freeze(ctypes.byref(a), _ptr(self.fa), _ptr(self.fb))
+        assert rc == 0, rc
+        return self
+
+    def forward(self, extra=None, want_hist=False, vp=None, eps=None, delta=None):
+        p = self.p
+        rec = np.zeros((p.nt, p.nx - 2 * p.pml, p.ny - 2 * p.pml), np.float64)
+        hist = np.zeros(p.N * p.nt, np.float64) if want_hist else None
+        a = self._args(vp, eps, delta)
+        ex = None if extra is None else np.ascontiguousarray(extra, np.float64).ravel()
+        rc = _adj_lib().oracle_adj_forward(ctypes.byref(a), _ptr(self.fa), _ptr(self.fb),
+                                           _ptr(ex), _ptr(rec), _ptr(hist))
+        assert rc == 0, rc
+        return (rec, hist) if want_hist else rec
+
+    def backward(self, hist, resid, want_fadj=False):
+        p = self.p
+        g = [np.zeros(p.N, np.float64) for _ in range(3)]
+        fadj = np.zeros(p.N * p.nt, np.float64) if want_fadj else None
+        a = self._args()
+        r = np.ascontiguousarray(resid, np.float64).ravel()
+        rc = _adj_lib().oracle_adj_backward(ctypes.byref(a), _ptr(self.fa), _ptr(self.fb),
+                                            _ptr(hist), _ptr(r), _ptr(g[0]), _ptr(g[1]),
+                                            _ptr(g[2]), _ptr(fadj))
+        assert rc == 0, rc
+        return (g, fadj) if want_fadj else g

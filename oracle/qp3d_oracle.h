@@ -98,6 +98,35 @@ void oracle_extend_model(const float *in, float *out, int nx, int ny, int nz,
                          int pml);               /* CPU_function.c:67-108 */
 float oracle_absmax(const float *a, size_t n);   /* CPU_function.c:10-22 */
 
+/* ---- FP64 adjoint (qp3d_adjoint.c) --------------------------------------
+ * The step with the scalar operator frozen per step and cell by the factors
+ * a = nx^2+ny^2, b = nz^2 of a base run (0 where it was below the
+ * threshold); model in double so that finite differences can perturb it.
+ * Volumes are padded [nz][nx][ny] doubles; per-step arrays nt * N. */
+typedef struct {
+    int nx, ny, nz, pml, sz, nt;
+    double dx, dy, dz, dt;
+    const double *vp, *eps, *del;        /* N each */
+    const float *source;                 /* N, or NULL */
+    const float *wavelet;                /* nt */
+    const float *dlr, *ddlr, *dtb, *ddtb, *dfb, *ddfb;
+    const float *c, *c2;
+    int nthreads;
+} oracle_adj_args;
+
+/* Base run with the live scalar operator: the frozen factors of every step. */
+int oracle_adj_freeze(const oracle_adj_args *a, double *fa, double *fb);
+/* Frozen-operator run: records (nt * hx * hy), and u^k before each step
+ * (nt * N) when u_hist is given; extra = nt * N additive sources or NULL. */
+int oracle_adj_forward(const oracle_adj_args *a, const double *fa, const double *fb,
+                       const double *extra, double *record, double *u_hist);
+/* Adjoint run for record residuals resid (nt * hx * hy): gradient of
+ * 1/2 |resid|^2 with respect to vp, eps, delta on the cells outside the PML
+ * shell (0 inside it), and the adjoint of the additive sources (nt * N). */
+int oracle_adj_backward(const oracle_adj_args *a, const double *fa, const double *fb,
+                        const double *u_hist, const double *resid, double *g_vp,
+                        double *g_eps, double *g_del, double *f_adj);
+
 #ifdef __cplusplus
 }
 #endif
