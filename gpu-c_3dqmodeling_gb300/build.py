@@ -28,6 +28,7 @@ SOURCES = [
     ("qp3d_api.cu", [NVCC] + CU_FLAGS),
     ("qp3d_noalloc.cu", [NVCC] + CU_FLAGS),
     ("qp3d_batch.cu", [NVCC] + CU_FLAGS),
+    ("qp3d_adjoint.cu", [NVCC] + CU_FLAGS),
     ("qp3d_host.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
                        "-Wall", "-I", INCLUDE, "-I", "/usr/local/cuda/include"]),
     ("qp3d_driver.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",

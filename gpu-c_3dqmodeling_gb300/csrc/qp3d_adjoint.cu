@@ -1,0 +1,231 @@
+// qp3d_adjoint.cu -- gradient of the L2 record misfit (qp3d_adjoint of
+// include/qp3d.h).  No counterpart in the reference.
+//
+// Operator: the forward step with its scalar operator S frozen per step and
+// cell (decision and unit normal from the forward wavefield, dependence on
+// eps and delta differentiated); with S frozen the step is linear in the
+// state (u, u_prev and the split-field PML state), and the adjoint is its
+// exact transpose (kernels qp3d_adj_a/b_kernel).  The FP64 oracle
+// (oracle/qp3d_adjoint.c) implements the same operator and passes
+// dot-product and finite-difference tests.
+//
+// Schedule: the forward pass stores the state every C = ceil(sqrt(nt)) steps
+// (nine volumes: u, u_prev, the live PML levels), in BF16 by default; the
+// backward pass restores each checkpoint, recomputes its C steps keeping
+// u^k in FP32, and runs the C adjoint steps backward.  Device memory:
+// ~27 + C volumes plus the checkpoints.  Gradients are summed per shot in
+// FP32 on the device and added to the caller's FP64 arrays.
+#include "qp3d_ctx.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+using namespace qp3d;
+
+// qp3d_api.cu
+int qp3d_internal_enqueue_step(qp3d_ctx *ctx);
+int qp3d_internal_restore_step(qp3d_ctx *ctx, int step);
+
+namespace qp3d {
+
+struct AdjState {
+    long long vol = 0;
+    int nt = 0, C = 0, nck = 0, bf16 = 1;
+    float *L[9] = {}, *N[9] = {}, *Cf[6] = {}, *g[3] = {};
+    float *seg = nullptr;          // C volumes: u^k of the segment
+    void *ck = nullptr;            // nck checkpoints x 9 volumes
+    float *resid = nullptr;        // nt * hx * hy
+    float *T2 = nullptr;
+};
+
+void adjoint_free(AdjState *s)
+{
+    if (!s) return;
+    for (auto *p : s->L) cudaFree(p);
+    for (auto *p : s->N) cudaFree(p);
+    for (auto *p : s->Cf) cudaFree(p);
+    for (auto *p : s->g) cudaFree(p);
+    cudaFree(s->seg);
+    cudaFree(s->ck);
+    cudaFree(s->resid);
+    cudaFree(s->T2);
+    delete s;
+}
+
+}  // namespace qp3d
+
+namespace {
+
+// The nine live state volumes at the start of step k (the rotation of
+// enqueue_step: PML levels k % 3 (old) and (k + 1) % 3 (current), W21 k % 2).
+void live_state(qp3d_ctx *ctx, int k, float *v[9])
+{
+    v[0] = ctx->U[ctx->cur];
+    v[1] = ctx->U[ctx->prev];
+    v[2] = ctx->W1[(k + 1) % 3];
+    v[3] = ctx->W1[k % 3];
+    v[4] = ctx->P[(k + 1) % 3];
+    v[5] = ctx->P[k % 3];
+    v[6] = ctx->W21[k % 2];
+    v[7] = ctx->W3[(k + 1) % 3];
+    v[8] = ctx->W3[k % 3];
+}
+
+int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, size_t rec)
+{
+    const size_t vb = (size_t)s->vol * sizeof(float);
+    for (int i = 0; i < 9; ++i) {
+        CK(cudaMalloc(&s->L[i], vb));
+        CK(cudaMalloc(&s->N[i], vb));
+    }
+    for (auto *&p : s->Cf) CK(cudaMalloc(&p, vb));
+    for (auto *&p : s->g) CK(cudaMalloc(&p, vb));
+    CK(cudaMalloc(&s->seg, vb * C));
+    const size_t es = bf16 ? sizeof(__nv_bfloat16) : sizeof(float);
+    CK(cudaMalloc(&s->ck, (size_t)s->vol * es * 9 * nck));
+    CK(cudaMalloc(&s->resid, rec * sizeof(float)));
+    CK(cudaMalloc(&s->T2, sizeof(float)));
+    s->C = C;
+    s->nck = nck;
+    s->bf16 = bf16;
+    return QP3D_OK;
+}
+
+}  // namespace
+
+extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m,
+                            const float *d_obs, double *grad_vp, double *grad_eps,
+                            double *grad_del, double *misfit)
+{
+    if (!ctx) return QP3D_ERR_ARG;
+    if (!g || !m || !d_obs) return ctx_fail(ctx, QP3D_ERR_ARG, "missing input");
+    if (ctx->param_fp16) return ctx_fail(ctx, QP3D_ERR_ARG, "qp3d_adjoint needs FP32 parameters");
+    int rc = qp3d_shot_load(ctx, g, m);
+    if (rc) return rc;
+    if (!ctx->fuse_sources || ctx->n_band > 0 || !ctx->rec_fused)
+        return ctx_fail(ctx, QP3D_ERR_ARG,
+                        "qp3d_adjoint: sources and receivers must lie inside the updated box");
+    const int nt = g->nt;
+    const long long vol = ctx->vol;
+    const size_t rec = (size_t)nt * ctx->hx * ctx->hy;
+    const int C = std::max(1, (int)std::ceil(std::sqrt((double)std::max(nt, 1))));
+    const int nck = (nt + C - 1) / C;
+    // state buffers, reused when the geometry repeats
+    AdjState *&S = ctx->adj;
+    if (S && (S->vol != vol || S->nt != nt || S->bf16 != ctx->adj_bf16)) {
+        adjoint_free(S);
+        S = nullptr;
+    }
+    if (!S) {
+        S = new (std::nothrow) AdjState();
+        if (!S) return ctx_fail(ctx, QP3D_ERR_NOMEM, "out of host memory");
+        S->vol = vol;
+        S->nt = nt;
+        if ((rc = alloc_state(ctx, S, C, nck, ctx->adj_bf16, rec))) {
+            adjoint_free(S);
+            S = nullptr;
+            return rc;
+        }
+    }
+    const size_t vb = (size_t)vol * sizeof(float);
+    const size_t es = S->bf16 ? sizeof(__nv_bfloat16) : sizeof(float);
+    auto ck_slot = [&](int c, int j) {
+        return static_cast<char *>(S->ck) + ((size_t)c * 9 + j) * (size_t)vol * es;
+    };
+
+    // ---- forward with checkpoints
+    for (int k = 0; k < nt; ++k) {
+        if (k % C == 0) {
+            float *v[9];
+            live_state(ctx, k, v);
+            for (int j = 0; j < 9; ++j) {
+                if (S->bf16)
+                    CKL(launch_to_bf16(v[j], reinterpret_cast<__nv_bfloat16 *>(ck_slot(k / C, j)),
+                                       vol, ctx->stream));
+                else
+                    CK(cudaMemcpyAsync(ck_slot(k / C, j), v[j], vb, cudaMemcpyDeviceToDevice,
+                                       ctx->stream));
+            }
+        }
+        if ((rc = qp3d_internal_enqueue_step(ctx))) return rc;
+    }
+    // ---- residual and misfit
+    std::vector<float> r(rec);
+    if ((rc = qp3d_shot_read_record(ctx, 0, nt, r.data()))) return rc;
+    double J = 0.0;
+    for (size_t i = 0; i < rec; ++i) {
+        r[i] -= d_obs[i];
+        J += 0.5 * (double)r[i] * r[i];
+    }
+    if (misfit) *misfit = J;
+    CK(cudaMemcpyAsync(S->resid, r.data(), rec * sizeof(float), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    for (auto *p : S->L) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
+    for (auto *p : S->g) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
+
+    // ---- backward, one checkpoint segment at a time
+    AdjParams a;
+    memset(&a, 0, sizeof(a));
+    a.nx = g->nx; a.ny = g->ny; a.nz = g->nz; a.ldy = ctx->ldy; a.pml = g->pml; a.sz = g->sz;
+    a.hx = ctx->hx; a.hy = ctx->hy; a.plane = ctx->plane; a.k = ctx->coefs; a.dt = g->dt;
+    a.K = ctx->K; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers; a.T2 = S->T2;
+    for (int c = nck - 1; c >= 0; --c) {
+        const int k0 = c * C, k1 = std::min(nt, k0 + C);
+        if ((rc = qp3d_internal_restore_step(ctx, k0))) return rc;
+        float *v[9];
+        live_state(ctx, k0, v);
+        for (int j = 0; j < 9; ++j) {
+            if (S->bf16)
+                CKL(launch_from_bf16(reinterpret_cast<const __nv_bfloat16 *>(ck_slot(c, j)), v[j],
+                                     vol, ctx->stream));
+            else
+                CK(cudaMemcpyAsync(v[j], ck_slot(c, j), vb, cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+        }
+        for (int k = k0; k < k1; ++k) {
+            CK(cudaMemcpyAsync(S->seg + (size_t)(k - k0) * vol, ctx->U[ctx->cur], vb,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+            if ((rc = qp3d_internal_enqueue_step(ctx))) return rc;
+        }
+        for (int k = k1 - 1; k >= k0; --k) {
+            CKL(launch_threshold(ctx->gmax + k, S->T2, ctx->stream));
+            a.u = S->seg + (size_t)(k - k0) * vol;
+            a.resid = S->resid + (size_t)k * ctx->hx * ctx->hy;
+            const float **Lc[9] = {&a.Lu, &a.Lup, &a.Lw1, &a.Lw1o, &a.Lp, &a.Lpo, &a.Lw21,
+                                   &a.Lw3, &a.Lw3o};
+            float **Nc[9] = {&a.Nu, &a.Nup, &a.Nw1, &a.Nw1o, &a.Np, &a.Npo, &a.Nw21, &a.Nw3,
+                             &a.Nw3o};
+            for (int j = 0; j < 9; ++j) {
+                *Lc[j] = S->L[j];
+                *Nc[j] = S->N[j];
+            }
+            for (int j = 0; j < 6; ++j) a.C[j] = S->Cf[j];
+            a.gK = S->g[0]; a.gE = S->g[1]; a.gD = S->g[2];
+            CKL(launch_adjoint_step(a, ctx->stream));
+            ++ctx->launches;   // two passes
+            for (int j = 0; j < 9; ++j) std::swap(S->L[j], S->N[j]);
+        }
+    }
+    // ---- gradient: interior cells, added to the caller's FP64 arrays
+    const int nx = g->nx, ny = g->ny, nz = g->nz, pml = g->pml;
+    std::vector<float> hg((size_t)nx * ny * nz);
+    double *outs[3] = {grad_vp, grad_eps, grad_del};
+    for (int q = 0; q < 3; ++q) {
+        if (!outs[q]) continue;
+        CK(cudaMemcpy2DAsync(hg.data(), (size_t)ny * 4, S->g[q], (size_t)ctx->ldy * 4,
+                             (size_t)ny * 4, (size_t)nx * nz, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int z = pml; z < nz - pml; ++z)
+            for (int x = pml; x < nx - pml; ++x)
+                for (int y = pml; y < ny - pml; ++y) {
+                    const size_t i = ((size_t)z * nx + x) * ny + y;
+                    double gi = hg[i];
+                    if (q == 0) gi *= 2.0 * (double)m->vp[i] * (double)g->dt * (double)g->dt;
+                    outs[q][i] += gi;
+                }
+    }
+    return qp3d_shot_sync(ctx);
+}

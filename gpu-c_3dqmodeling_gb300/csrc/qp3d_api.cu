@@ -121,6 +121,8 @@ extern "C" void qp3d_ctx_destroy(qp3d_ctx *ctx)
     free_shot(ctx);
     batch_free(ctx->batch);
     ctx->batch = nullptr;
+    adjoint_free(ctx->adj);
+    ctx->adj = nullptr;
     if (ctx->errword) cudaFree(ctx->errword);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
@@ -469,6 +471,31 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     ctx->prev = a;
     ctx->cur = c;
     ctx->step = k + 1;
+    return QP3D_OK;
+}
+
+// For qp3d_adjoint.cu: one step of the loaded shot, and a jump back to the
+// start of step `step` (rotation as from a reset; the per-step bookkeeping
+// of the steps to come is cleared; the caller restores the state volumes).
+int qp3d_internal_enqueue_step(qp3d_ctx *ctx)
+{
+    if (ctx->step >= ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_STATE, "step past nt");
+    return enqueue_step(ctx, nullptr, nullptr, nullptr, nullptr);
+}
+
+int qp3d_internal_restore_step(qp3d_ctx *ctx, int step)
+{
+    if (step < 0 || step >= ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "bad step %d", step);
+    const size_t n = (size_t)(ctx->g.nt - step);
+    CK(cudaMemsetAsync(ctx->gmax + step, 0, n * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(ctx->win + 3 * (size_t)step, 0, 3 * n * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(ctx->redo + step, 0, n * sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->alt_count + step, 0, n * sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->fix_count + step, 0, n * sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->sres + 2 * (size_t)step, 0, 2 * n * sizeof(float), ctx->stream));
+    ctx->step = step;
+    ctx->cur = (3 - step % 3) % 3;
+    ctx->prev = (ctx->cur + 1) % 3;
     return QP3D_OK;
 }
 
@@ -836,6 +863,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "spec_bias_ppm") && value >= -500000 && value <= 1000000)
         ctx->spec_bias = value * 1e-6f;
     else if (!strcmp(key, "param_fp16") && (value == 0 || value == 1)) ctx->param_fp16 = value;
+    else if (!strcmp(key, "adj_ckpt_bf16") && (value == 0 || value == 1)) ctx->adj_bf16 = value;
     else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
     if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
         CK(cudaSetDevice(ctx->device));
@@ -858,6 +886,7 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "spec_delta_ppm")) return (int)(ctx->delta_min * 1e6f + 0.5f);
     if (!strcmp(key, "spec_bias_ppm")) return (int)lrintf(ctx->spec_bias * 1e6f);
     if (!strcmp(key, "param_fp16")) return ctx->param_fp16;
+    if (!strcmp(key, "adj_ckpt_bf16")) return ctx->adj_bf16;
     if (!strcmp(key, "batch_graph")) return ctx->batch_graph;
     if (!strcmp(key, "batch_tune")) return ctx->batch_tune;
     if (!strcmp(key, "batch_candidate")) return ctx->batch_candidate;

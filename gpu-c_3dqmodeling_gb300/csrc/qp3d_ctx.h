@@ -14,6 +14,8 @@ void derive_coefs(const float *c, const float *c2, float dx, float dy, float dz,
 void derive_layers(const float *d, const float *dd, int pml, float dt, float4 *out);
 struct BatchState;                 // qp3d_batch.cu
 void batch_free(BatchState *b);
+struct AdjState;                   // qp3d_adjoint.cu
+void adjoint_free(AdjState *s);
 }  // namespace qp3d
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -85,6 +87,9 @@ struct qp3d_ctx {
     int batch_tune = 1;              // choose the tile / z-block shape by timing
     int batch_candidate = -1;        // fixed shape (when not tuning), -1: default
     long long batch_mem_mb = 0;      // device memory for one group of shots, 0: auto
+    // adjoint (qp3d_adjoint)
+    qp3d::AdjState *adj = nullptr;
+    int adj_bf16 = 1;                // checkpoints in BF16 (0: FP32, exact recompute)
 };
 inline int ctx_fail(qp3d_ctx *c, int code, const char *fmt, ...)
 {

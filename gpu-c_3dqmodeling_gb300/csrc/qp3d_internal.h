@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -161,6 +162,31 @@ struct BatchArgs {
     int nwork;
     int *queue;               // next work item (zeroed by the prepare kernel)
 };
+
+// One backward step of the adjoint (qp3d_adjoint.cu): the adjoint state of
+// s^{k+1} (L*) to that of s^k (N*), with the scalar operator of step k frozen
+// from u^k and the step's threshold.  C: coefficient fields of the
+// transposed derivatives (x, y, z first; xx, yy, zz second).
+struct AdjParams {
+    int nx, ny, nz, ldy, pml, sz, hx, hy;
+    long long plane;
+    Coefs k;
+    float dt;
+    const float *u;                        // u^k
+    const float *K, *E2, *R8;              // (vp dt)^2, 2 eps, 8 (eps - delta)
+    const float4 *layers;
+    const float *T2;                       // threshold m2 of step k
+    const float *resid;                    // record residual of step k (hx * hy)
+    const float *Lu, *Lup, *Lw1, *Lw1o, *Lp, *Lpo, *Lw21, *Lw3, *Lw3o;
+    float *Nu, *Nup, *Nw1, *Nw1o, *Np, *Npo, *Nw21, *Nw3, *Nw3o;
+    float *C[6];
+    float *gK, *gE, *gD;                   // gradient sums over the steps
+};
+
+cudaError_t launch_adjoint_step(const AdjParams &a, cudaStream_t stream);
+cudaError_t launch_threshold(const float *gmax_k, float *T2, cudaStream_t stream);
+cudaError_t launch_to_bf16(const float *a, __nv_bfloat16 *h, long long n, cudaStream_t stream);
+cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cudaStream_t stream);
 
 struct Shot;   // host-side, defined in qp3d_api.cu
 

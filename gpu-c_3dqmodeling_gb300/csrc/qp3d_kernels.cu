@@ -1518,6 +1518,137 @@ __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
                gridDim.x);
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint (qp3d_adjoint.cu drives them).  Pass A, per cell: the residual of
+// the step is injected at the receivers; the scalar operator of step k is
+// rebuilt from u^k (frozen: its decision and unit normal are those of the
+// forward, its eps/delta dependence is differentiated); the PML recursions
+// and the interior leapfrog are transposed term by term; each derivative the
+// update took of u^k leaves a coefficient field; the gradient terms
+// lambda * (d update / d m) are summed.  Pass B, per cell: the transposed
+// stencils of the six coefficient fields (second derivatives: the stencil
+// itself; first derivatives: its negative), zero outside the volume.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
+{
+    const int y = blockIdx.x * 32 + threadIdx.x, x = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+    if (y >= a.ny || x >= a.nx) return;
+    const long long i = (long long)z * a.plane + (long long)x * a.ldy + y;
+    const int nx = a.nx, ny = a.ny, nz = a.nz, pml = a.pml;
+    float l = a.Lu[i];
+    if (a.resid && z == a.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
+        l += a.resid[(long long)(x - pml) * a.hy + (y - pml)];
+    float nu = a.Lup[i], nup = 0.f, nw1 = 0.f, nw1o = 0.f, np_ = 0.f, npo = 0.f, nw21 = 0.f,
+          nw3 = 0.f, nw3o = 0.f;
+    float c[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const bool upd = x >= kRadius && x < nx - kRadius && y >= kRadius && y < ny - kRadius &&
+                     z >= kRadius && z < nz - kRadius;
+    if (!upd) {
+        nu += l;   // a never-updated cell keeps its value
+    } else {
+        float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
+        cell_derivs(a.u, i, a.ldy, a.plane, a.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        const float K = a.K[i], E2 = a.E2[i], R8 = a.R8[i], e2 = 1.0f + E2;
+        const float h2 = fmaf(Uy, Uy, Ux * Ux), m2 = fmaf(Uz, Uz, h2);
+        float S = 1.0f, dSe = 0.0f, dSd = 0.0f;
+        if (m2 > *a.T2) {
+            const float aa = h2 / m2, bb = 1.0f - aa, D = fmaf(E2, aa, 1.0f);
+            const float ab8 = 8.0f * aa * bb / (D * D);
+            const float q = 0.125f * R8 * ab8;
+            const float r = sqrtf(fmaxf(1.0f - q, 0.0f));
+            S = 0.5f + 0.5f * r;
+            const float dSdq = r > 0.0f ? -0.25f / r : 0.0f;
+            dSe = dSdq * ab8 * (1.0f - aa * R8 / (2.0f * D));
+            dSd = -dSdq * ab8;
+        }
+        const float KS = K * S;
+        const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
+        const int fy = y < pml ? 2 : (y >= ny - pml ? 3 : -1);
+        const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
+        int f, li;
+        cell_face(fx, x < pml ? pml - x : x - nx + pml, fy, y < pml ? pml - y : y - ny + pml, fz,
+                  z < pml ? pml - z : z - nz + pml, f, li);
+        if (f < 0) {
+            nu += 2.0f * l;
+            nup = -l;
+            c[3] = KS * e2 * l;
+            c[4] = c[3];
+            c[5] = KS * l;
+            const float Lh = Uxx + Uyy, Lap = fmaf(e2, Lh, Uzz);
+            a.gK[i] += l * S * Lap;
+            a.gE[i] += l * K * (2.0f * S * Lh + dSe * Lap);
+            a.gD[i] += l * K * dSd * Lap;
+        } else {
+            const float4 lc = a.layers[(f >> 1) * pml + li];
+            const bool isz = f >= 4;
+            const float A = isz ? KS : e2 * KS, Bt = isz ? e2 * KS : KS;
+            const float sgn = (f & 1) ? -1.0f : 1.0f;
+            const float W1 = a.Lw1[i] + l, W21 = a.Lw21[i] + l, W3 = a.Lw3[i] + l;
+            const float P = fmaf(a.dt, W21, a.Lp[i]);
+            nw1 = fmaf(-lc.x, W1, a.Lw1o[i]);
+            nw1o = lc.y * W1;
+            np_ = fmaf(-lc.x, P, a.Lpo[i]);
+            npo = lc.y * P;
+            nw21 = lc.z * W21;
+            nw3 = fmaf(2.0f, W3, a.Lw3o[i]);
+            nw3o = -W3;
+            const float cn = A * W1, c1 = sgn * A * lc.w * P, ct = Bt * W3;
+            if (f < 2) { c[3] += cn; c[0] += c1; c[4] += ct * e2; c[5] += ct; }
+            else if (f < 4) { c[4] += cn; c[1] += c1; c[3] += ct * e2; c[5] += ct; }
+            else { c[5] += cn; c[2] += c1; c[3] += ct; c[4] += ct; }
+        }
+    }
+    a.Nu[i] = nu; a.Nup[i] = nup;
+    a.Nw1[i] = nw1; a.Nw1o[i] = nw1o; a.Np[i] = np_; a.Npo[i] = npo;
+    a.Nw21[i] = nw21; a.Nw3[i] = nw3; a.Nw3o[i] = nw3o;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) a.C[j][i] = c[j];
+}
+
+__global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
+{
+    const int y = blockIdx.x * 32 + threadIdx.x, x = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+    if (y >= a.ny || x >= a.nx) return;
+    const long long i = (long long)z * a.plane + (long long)x * a.ldy + y;
+    const float *Cx = a.C[0], *Cy = a.C[1], *Cz = a.C[2], *Cxx = a.C[3], *Cyy = a.C[4],
+                *Czz = a.C[5];
+    const Coefs &k = a.k;
+    float acc = k.kx * Cxx[i] + k.ky * Cyy[i] + k.kz * Czz[i];
+#pragma unroll
+    for (int m = 0; m < kRadius; ++m) {
+        const int d = m + 1;
+        float sxx = 0.f, sx = 0.f, syy = 0.f, sy = 0.f, szz = 0.f, sz = 0.f;
+        if (x + d < a.nx) { const long long j = i + (long long)d * a.ldy; sxx += Cxx[j]; sx -= Cx[j]; }
+        if (x - d >= 0) { const long long j = i - (long long)d * a.ldy; sxx += Cxx[j]; sx += Cx[j]; }
+        if (y + d < a.ny) { syy += Cyy[i + d]; sy -= Cy[i + d]; }
+        if (y - d >= 0) { syy += Cyy[i - d]; sy += Cy[i - d]; }
+        if (z + d < a.nz) { const long long j = i + (long long)d * a.plane; szz += Czz[j]; sz -= Cz[j]; }
+        if (z - d >= 0) { const long long j = i - (long long)d * a.plane; szz += Czz[j]; sz += Cz[j]; }
+        acc += k.c2x[m] * sxx + k.c2y[m] * syy + k.c2z[m] * szz + k.cx[m] * sx + k.cy[m] * sy +
+               k.cz[m] * sz;
+    }
+    a.Nu[i] += acc;
+}
+
+__global__ void qp3d_threshold_kernel(const float *gmax_k, float *T2)
+{
+    if (threadIdx.x == 0) *T2 = threshold_m2(*gmax_k);
+}
+
+__global__ void qp3d_to_bf16_kernel(const float *a, __nv_bfloat16 *h, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        h[i] = __float2bfloat16_rn(a[i]);
+}
+
+__global__ void qp3d_from_bf16_kernel(const __nv_bfloat16 *h, float *a, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        a[i] = __bfloat162float(h[i]);
+}
+
 __global__ void qp3d_to_half_kernel(const float *a, __half *h, long long n)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -1694,6 +1825,36 @@ cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0, int 
     long long b = (n + 255) / 256;
     int blocks = (int)(b > 8192 ? 8192 : b);
     qp3d_crop_kernel<<<blocks, 256, 0, stream>>>(u, out, x0, x1, y0, y1, z0, z1, ldy, plane);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_step(const AdjParams &a, cudaStream_t stream)
+{
+    const dim3 block(32, 8), grid((a.ny + 31) / 32, (a.nx + 7) / 8, a.nz);
+    qp3d_adj_a_kernel<<<grid, block, 0, stream>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    qp3d_adj_b_kernel<<<grid, block, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_threshold(const float *gmax_k, float *T2, cudaStream_t stream)
+{
+    qp3d_threshold_kernel<<<1, 32, 0, stream>>>(gmax_k, T2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float *a, __nv_bfloat16 *h, long long n, cudaStream_t stream)
+{
+    long long b = (n + 255) / 256;
+    qp3d_to_bf16_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(a, h, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cudaStream_t stream)
+{
+    long long b = (n + 255) / 256;
+    qp3d_from_bf16_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(h, a, n);
     return cudaGetLastError();
 }
 

@@ -95,7 +95,7 @@ class RunOptions(ctypes.Structure):
 # every symbol include/qp3d.h and include/qp3d_driver.h declare
 EXPORTS = [
     "qp3d_version", "qp3d_strerror", "qp3d_ctx_create", "qp3d_ctx_destroy",
-    "qp3d_ctx_last_error", "qp3d_forward", "qp3d_batch", "qp3d_batch_get_stats", "qp3d_shot_load", "qp3d_shot_reset",
+    "qp3d_ctx_last_error", "qp3d_forward", "qp3d_adjoint", "qp3d_batch", "qp3d_batch_get_stats", "qp3d_shot_load", "qp3d_shot_reset",
     "qp3d_shot_advance", "qp3d_shot_sync", "qp3d_shot_step", "qp3d_shot_read_record",
     "qp3d_shot_read_uxyzmax", "qp3d_shot_read_stats", "qp3d_shot_snapshot", "qp3d_pml_state_size",
     "qp3d_shot_write_state", "qp3d_shot_read_state", "qp3d_shot_time",
@@ -126,6 +126,7 @@ def load():
         "qp3d_ctx_last_error": (ctypes.c_char_p, [_vp]),
         "qp3d_forward": (ctypes.c_int, [_vp, P(Geom), P(Model), _vp, P(Snap)]),
         "qp3d_batch": (ctypes.c_int, [_vp, ctypes.c_int, P(ShotDesc)]),
+        "qp3d_adjoint": (ctypes.c_int, [_vp, P(Geom), P(Model), _vp, _vp, _vp, _vp, _vp]),
         "qp3d_batch_get_stats": (ctypes.c_int, [_vp, P(BatchStats)]),
         "qp3d_shot_load": (ctypes.c_int, [_vp, P(Geom), P(Model)]),
         "qp3d_shot_reset": (ctypes.c_int, [_vp]),
@@ -369,6 +370,23 @@ class Context:
         self._shot = None
         self._check(self._L.qp3d_batch(self.h, len(shots), arr), "qp3d_batch")
         return records
+
+    def adjoint(self, shot, d_obs, grads=None):
+        """qp3d_adjoint: (misfit, [g_vp, g_eps, g_delta]) with the gradients
+        added to grads (three float64 arrays of shot.N) when given."""
+        if grads is None:
+            grads = [np.zeros(shot.N, np.float64) for _ in range(3)]
+        d = np.ascontiguousarray(d_obs, np.float32)
+        if d.size != shot.nt * shot.hx * shot.hy:
+            raise ValueError("d_obs must hold nt*hx*hy samples")
+        J = ctypes.c_double()
+        g, m = shot.geom(), shot.model()
+        self._shot = None
+        self._check(self._L.qp3d_adjoint(self.h, ctypes.byref(g), ctypes.byref(m), _p(d),
+                                          _p(grads[0]), _p(grads[1]), _p(grads[2]),
+                                          ctypes.byref(J)), "qp3d_adjoint")
+        self._shot = shot
+        return J.value, grads
 
     def batch_stats(self):
         st = BatchStats()

@@ -17,6 +17,7 @@
  *                             CPU impl modeling3D.c:17-153)
  *   qp3d_shot_* ............. the same call split into load / advance / read
  *                             so that callers can keep the model resident
+ *   qp3d_adjoint ............ no counterpart (gradient of the record misfit)
  *   qp3d_batch .............. the shot loop of the main programs
  *                             (3dPureqPModeling1.0.c:225-277, Main.c:181-231),
  *                             one modeling3d call per shot there
@@ -138,6 +139,23 @@ typedef struct {
 } qp3d_batch_stats;
 int qp3d_batch_get_stats(const qp3d_ctx *ctx, qp3d_batch_stats *out);
 
+/* Gradient of the record misfit J = 1/2 sum |record - d_obs|^2 of one shot
+ * with respect to vp, epsilon and delta, by the adjoint-state method.  No
+ * counterpart in the reference.  The forward is the qp3d_forward step with
+ * its scalar operator S frozen per step and cell (threshold decision and
+ * unit normal of the forward wavefield; S's dependence on epsilon and delta
+ * is differentiated); the adjoint is the exact transpose of that step,
+ * split-field PML included.  Checkpoints every ceil(sqrt(nt)) steps, stored
+ * in BF16 ("adj_ckpt_bf16" = 0: FP32, recompute bit-identical to the
+ * forward).  The gradient is added (+=) to the caller's padded [nz][nx][ny]
+ * FP64 arrays on the cells outside the PML shell (the shell's parameters
+ * extend the interior edge and are held fixed); NULL skips one.  misfit:
+ * out, J (may be NULL).  Needs FP32 parameter storage and sources and
+ * receivers inside the updated box; replaces the loaded shot. */
+int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m,
+                 const float *d_obs, double *grad_vp, double *grad_eps,
+                 double *grad_del, double *misfit);
+
 /* Staged form of the same shot. */
 int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model *m);
 int qp3d_shot_reset(qp3d_ctx *ctx);                 /* zero state, step 0 */
@@ -194,7 +212,8 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * results.  "param_fp16" (1: the next qp3d_shot_load / qp3d_forward stores
  * vp, epsilon and delta as IEEE half, rounded to nearest; the stencil stays
  * FP32, and the results equal an FP32 run on the rounded model bit for bit;
- * qp3d_batch always stores FP32). */
+ * qp3d_batch always stores FP32).  "adj_ckpt_bf16" (qp3d_adjoint
+ * checkpoint storage, 1: BF16, 0: FP32). */
 int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
 int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
 
