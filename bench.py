@@ -32,6 +32,13 @@ Nz0 in [128, 200], 20-cell PML, 10.8 M padded cells on average) cut from one
   single_shot_form  the same shots one qp3d call each: device time of the
              resident time loop and wall time of qp3d_forward
 
+--workload adjoint measures the misfit gradient (qp3d_adjoint): a 12-layer
+200x200x150 true model (+20-cell PML, 240x240x190 padded) and a start model
+smoothed by a 3D Gaussian of 5 cells, 16 shots on a 4x4 surface grid, 2000
+steps, sqrt(nt) checkpoints in BF16 (and FP32 beside it); value = seconds per
+shot of the gradient (forward, residual, checkpointed backward), the records
+of the true model made first.
+
 --workload large measures the large mixed-precision configuration (one bench
 step = one shot): 800x800x400 cells + 40-cell PML (880x880x480 padded, 372 M
 cells), 20 dipping layers and 30 Gaussian velocity anomalies, 5000 steps,
@@ -73,7 +80,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="scale the horizontal/vertical extent (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "large"])
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "batch", "large", "adjoint"])
     ap.add_argument("--shots", type=int, default=64, help="batch workload: shots")
     return ap.parse_args()
 
@@ -557,6 +565,74 @@ def run_large_arm(args, dist):
     return 0
 
 
+ADJ_NAME = ("misfit gradient: 12-layer 200x200x150 true model (+20-cell PML), start model "
+            "smoothed by a 3D Gaussian (sigma 5 cells), %d shots on a 4x4 surface grid, %d "
+            "steps x 0.5 ms, 20 Hz, surface receivers, sqrt(nt) checkpoints")
+
+
+def run_adjoint_arm(args, dist):
+    import qp3d
+    import synthetic
+    nt = args.nt if args.nt is not None else 2000
+    true, start = synthetic.adjoint_case(nt=nt)
+    ctx = qp3d.Context(dist.local)
+    d_obs = [ctx.forward(s).copy() for s in true]
+    N = start[0].N
+    res = {}
+    gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
+                 if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
+    clocks = Clocks(gpu_index)
+    launches0 = ctx.launch_count()
+    for name, bf16 in (("bf16_checkpoints", 1), ("fp32_checkpoints", 0)):
+        ctx.tune(adj_ckpt_bf16=bf16)
+        for _ in range(args.warmup):
+            ctx.adjoint(start[0], d_obs[0])
+        grads = [np.zeros(N, np.float64) for _ in range(3)]
+        J = 0.0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for s, d in zip(start, d_obs):
+                j, _ = ctx.adjoint(s, d, grads)
+                J += j
+        sec = time.perf_counter() - t0
+        res[name] = {"s_per_shot": round(sec / (args.steps * len(start)), 4),
+                     "misfit": J / args.steps, "grads": grads}
+    clk = clocks.stop()
+    gpu_launches = ctx.launch_count() - launches0
+    cos = {}
+    for i, p in enumerate(("vp", "eps", "delta")):
+        a, b = res["bf16_checkpoints"]["grads"][i], res["fp32_checkpoints"]["grads"][i]
+        cos[p] = round(float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b))), 6)
+    t_fwd = None
+    ctx.load(start[0])
+    tot, _, _ = ctx.time(nt, per_kernel=False)
+    t_fwd = tot / 1e3
+    if dist.rank == 0:
+        line = {
+            "metric": "adjoint grad s/shot", "value": res["bf16_checkpoints"]["s_per_shot"],
+            "unit": "s/shot", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * res["bf16_checkpoints"]["s_per_shot"]
+                                                        * len(start), 1),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": ADJ_NAME % (len(start), nt),
+                       "step": "gradient of all %d shots" % len(start),
+                       "grid": [start[0].nx, start[0].ny, start[0].nz], "nt": nt,
+                       "parallelism": "single"},
+            "fp32_checkpoints_s_per_shot": res["fp32_checkpoints"]["s_per_shot"],
+            "forward_only_s_per_shot": round(t_fwd, 4),
+            "misfit": res["bf16_checkpoints"]["misfit"],
+            "cosine_bf16_vs_fp32_checkpoints": cos,
+            "e2e": {"value": res["bf16_checkpoints"]["s_per_shot"], "unit": "s/shot",
+                    "note": "host model in, host FP64 gradient out"},
+            "gpu_launches": gpu_launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -567,6 +643,8 @@ def main():
             return run_batch_arm(args, dist)
         if args.workload == "large":
             return run_large_arm(args, dist)
+        if args.workload == "adjoint":
+            return run_adjoint_arm(args, dist)
         return run_gpu_arm(args, dist)
     finally:
         dist.close()

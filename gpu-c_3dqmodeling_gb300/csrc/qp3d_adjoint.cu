@@ -10,9 +10,18 @@
 // dot-product and finite-difference tests.
 //
 // Schedule: the forward pass stores the state every C = ceil(sqrt(nt)) steps
-// (nine volumes: u, u_prev, the live PML levels), in BF16 by default; the
-// backward pass restores each checkpoint, recomputes its C steps keeping
-// u^k in FP32, and runs the C adjoint steps backward.  Device memory:
+// (nine volumes: u, u_prev and the seven live PML levels), in FP32 by default
+// so that the recomputation is bit-identical to the forward; the backward
+// pass restores each checkpoint, recomputes its C steps keeping u^k, and runs
+// the C adjoint steps backward.  With "adj_ckpt_bf16" the PML levels are kept
+// in BF16 (22 instead of 36 bytes per cell and checkpoint); u always stays
+// FP32 because S depends on the direction of grad u, a difference of
+// neighbouring values that BF16 rounding of a smooth wavefield destroys.  The
+// delta gradient lives in S, whose threshold decision is a discontinuity, so
+// it is the component most sensitive to any change of the recomputed
+// wavefield (measured on 16 shots of 240x240x190: cosine against FP32
+// checkpoints 0.999999 vp, 0.99997 eps, 0.91 delta with BF16 PML levels,
+// 0.87 delta with an all-BF16 state).  Device memory:
 // ~27 + C volumes plus the checkpoints.  Gradients are summed per shot in
 // FP32 on the device and added to the caller's FP64 arrays.
 #include "qp3d_ctx.h"
@@ -83,8 +92,9 @@ int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, size_t rec
     for (auto *&p : s->Cf) CK(cudaMalloc(&p, vb));
     for (auto *&p : s->g) CK(cudaMalloc(&p, vb));
     CK(cudaMalloc(&s->seg, vb * C));
-    const size_t es = bf16 ? sizeof(__nv_bfloat16) : sizeof(float);
-    CK(cudaMalloc(&s->ck, (size_t)s->vol * es * 9 * nck));
+    const size_t per = (size_t)s->vol * (bf16 ? 2 * sizeof(float) + 7 * sizeof(__nv_bfloat16)
+                                              : 9 * sizeof(float));
+    CK(cudaMalloc(&s->ck, per * nck));
     CK(cudaMalloc(&s->resid, rec * sizeof(float)));
     CK(cudaMalloc(&s->T2, sizeof(float)));
     s->C = C;
@@ -130,9 +140,11 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
         }
     }
     const size_t vb = (size_t)vol * sizeof(float);
-    const size_t es = S->bf16 ? sizeof(__nv_bfloat16) : sizeof(float);
+    // checkpoint c: volumes 0, 1 (u, u_prev) FP32, 2..8 FP32 or BF16
+    const size_t hb = S->bf16 ? (size_t)vol * sizeof(__nv_bfloat16) : vb;
     auto ck_slot = [&](int c, int j) {
-        return static_cast<char *>(S->ck) + ((size_t)c * 9 + j) * (size_t)vol * es;
+        return static_cast<char *>(S->ck) + (size_t)c * (2 * vb + 7 * hb) +
+               (j < 2 ? (size_t)j * vb : 2 * vb + (size_t)(j - 2) * hb);
     };
 
     // ---- forward with checkpoints
@@ -141,7 +153,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
             float *v[9];
             live_state(ctx, k, v);
             for (int j = 0; j < 9; ++j) {
-                if (S->bf16)
+                if (S->bf16 && j >= 2)
                     CKL(launch_to_bf16(v[j], reinterpret_cast<__nv_bfloat16 *>(ck_slot(k / C, j)),
                                        vol, ctx->stream));
                 else
@@ -177,7 +189,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
         float *v[9];
         live_state(ctx, k0, v);
         for (int j = 0; j < 9; ++j) {
-            if (S->bf16)
+            if (S->bf16 && j >= 2)
                 CKL(launch_from_bf16(reinterpret_cast<const __nv_bfloat16 *>(ck_slot(c, j)), v[j],
                                      vol, ctx->stream));
             else

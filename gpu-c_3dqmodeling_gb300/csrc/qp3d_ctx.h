@@ -89,7 +89,7 @@ struct qp3d_ctx {
     long long batch_mem_mb = 0;      // device memory for one group of shots, 0: auto
     // adjoint (qp3d_adjoint)
     qp3d::AdjState *adj = nullptr;
-    int adj_bf16 = 1;                // checkpoints in BF16 (0: FP32, exact recompute)
+    int adj_bf16 = 0;                // 1: PML levels of the checkpoints in BF16
 };
 inline int ctx_fail(qp3d_ctx *c, int code, const char *fmt, ...)
 {

@@ -113,6 +113,26 @@ def large_vti(hx=800, hy=800, nz0=400, pml=40, nt=5000, dx=10.0, dt=5e-4, fm=20.
     return _finish(vp, eps, de, pml, dx * decimate, dt, nt, fm)
 
 
+def adjoint_case(hx=200, hy=200, nz0=150, pml=20, nt=2000, dx=10.0, dt=5e-4, fm=20.0, seed=4,
+                 sigma=5.0, grid=4):
+    """Gradient workload: a true layered model (layered_volume) and a start
+    model smoothed by a 3D Gaussian of sigma cells, with grid x grid shots on
+    the surface (sources at the centres of a regular grid of the top face,
+    receivers on that face).  Returns (true_shots, start_shots)."""
+    from scipy.ndimage import gaussian_filter
+    vp, eps, de = layered_volume(hx, hy, nz0, 12, seed, 0.15)
+    smooth = [gaussian_filter(a.astype(np.float64), sigma, mode="nearest").astype(np.float32)
+              for a in (vp, eps, de)]
+    pos = [int((i + 0.5) * hx / grid) for i in range(grid)]
+    posy = [int((i + 0.5) * hy / grid) for i in range(grid)]
+    true, start = [], []
+    for sx in pos:
+        for sy in posy:
+            true.append(_finish(vp, eps, de, pml, dx, dt, nt, fm, src_xyz=(sx, sy, 0)))
+            start.append(_finish(*smooth, pml, dx, dt, nt, fm, src_xyz=(sx, sy, 0)))
+    return true, start
+
+
 def batch_windows(nshots=64, seed=3, model=(512, 512, 200), hrange=(128, 256),
                   zrange=(128, 200), frange=(15.0, 30.0)):
     """Apertures of the batched workload: per shot (x0, y0, hx, hy, nz0, fm)

@@ -145,9 +145,10 @@ int qp3d_batch_get_stats(const qp3d_ctx *ctx, qp3d_batch_stats *out);
  * its scalar operator S frozen per step and cell (threshold decision and
  * unit normal of the forward wavefield; S's dependence on epsilon and delta
  * is differentiated); the adjoint is the exact transpose of that step,
- * split-field PML included.  Checkpoints every ceil(sqrt(nt)) steps, stored
- * in BF16 ("adj_ckpt_bf16" = 0: FP32, recompute bit-identical to the
- * forward).  The gradient is added (+=) to the caller's padded [nz][nx][ny]
+ * split-field PML included.  Checkpoints every ceil(sqrt(nt)) steps, FP32 by
+ * default (the recomputation is bit-identical to the forward);
+ * "adj_ckpt_bf16" = 1 keeps the seven PML state levels in BF16 (u and u_prev
+ * stay FP32), which perturbs mostly the delta gradient.  The gradient is added (+=) to the caller's padded [nz][nx][ny]
  * FP64 arrays on the cells outside the PML shell (the shell's parameters
  * extend the interior edge and are held fixed); NULL skips one.  misfit:
  * out, J (may be NULL).  Needs FP32 parameter storage and sources and
@@ -213,7 +214,7 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * vp, epsilon and delta as IEEE half, rounded to nearest; the stencil stays
  * FP32, and the results equal an FP32 run on the rounded model bit for bit;
  * qp3d_batch always stores FP32).  "adj_ckpt_bf16" (qp3d_adjoint
- * checkpoint storage, 1: BF16, 0: FP32). */
+ * checkpoint storage of the PML state, 0: FP32 (default), 1: BF16). */
 int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
 int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
 
