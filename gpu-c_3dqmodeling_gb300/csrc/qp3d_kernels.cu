@@ -799,6 +799,34 @@ __device__ __forceinline__ float rcp_nr(float x)
     return r;
 }
 
+// The same two operations on a pair of cells with the packed FP32x2
+// instructions (round-to-nearest per lane: each lane is bit-identical to the
+// scalar form).
+__device__ __forceinline__ float2 rcp_nr2(float2 x)
+{
+    float2 r = make_float2(__uint_as_float(0x7EF311C3u - __float_as_uint(x.x)),
+                           __uint_as_float(0x7EF311C3u - __float_as_uint(x.y)));
+    const float2 nx = make_float2(-x.x, -x.y), one = make_float2(1.0f, 1.0f);
+#pragma unroll
+    for (int it = 0; it < 3; ++it) {
+        const float2 e = __ffma2_rn(nx, r, one);
+        r = __ffma2_rn(r, e, r);
+    }
+    return r;
+}
+
+__device__ __forceinline__ float2 aniso_s2(float2 h2, float2 m2, float2 e2x, float2 r8)
+{
+    const float2 one = make_float2(1.0f, 1.0f), half = make_float2(0.5f, 0.5f);
+    const float2 aa = __fmul2_rn(h2, rcp_nr2(m2));
+    const float2 bb = __fadd2_rn(one, make_float2(-aa.x, -aa.y));
+    const float2 den = __ffma2_rn(e2x, aa, one);
+    const float2 num = __fmul2_rn(__fmul2_rn(r8, aa), bb);
+    const float2 qq = __fmul2_rn(num, rcp_nr2(__fmul2_rn(den, den)));
+    const float2 t = __fadd2_rn(one, make_float2(-qq.x, -qq.y));
+    return __ffma2_rn(half, make_float2(__fsqrt_rn(t.x), __fsqrt_rn(t.y)), half);
+}
+
 // S of one cell (GPU_kernel.cu:100-111), given it is above the threshold:
 // with a = (nx^2 + ny^2) = h2/m2 and nz^2 = 1 - a,
 // S = 1/2 + 1/2 sqrt(1 - 8(eps-delta) a (1-a) / (1 + 2 eps a)^2).
@@ -985,9 +1013,13 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         float KS[4], e2[4];
         if (__any_sync(0xffffffffu, any_above)) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const float s = aniso_s(h2[j], m2[j], f4(Ev, j), f4(Rv, j));
-                KS[j] = __fmul_rn(f4(Kv, j), above[j] ? s : 1.0f);
+            for (int h = 0; h < 2; ++h) {   // cells (0,1) and (2,3) as pairs
+                const int j0 = 2 * h, j1 = 2 * h + 1;
+                const float2 s = aniso_s2(make_float2(h2[j0], h2[j1]), make_float2(m2[j0], m2[j1]),
+                                          make_float2(f4(Ev, j0), f4(Ev, j1)),
+                                          make_float2(f4(Rv, j0), f4(Rv, j1)));
+                KS[j0] = __fmul_rn(f4(Kv, j0), above[j0] ? s.x : 1.0f);
+                KS[j1] = __fmul_rn(f4(Kv, j1), above[j1] ? s.y : 1.0f);
             }
         } else {
 #pragma unroll
