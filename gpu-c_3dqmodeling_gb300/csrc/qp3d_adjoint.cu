@@ -174,7 +174,11 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     if (misfit) *misfit = J;
     CK(cudaMemcpyAsync(S->resid, r.data(), rec * sizeof(float), cudaMemcpyHostToDevice,
                        ctx->stream));
+    // every entry the adjoint kernels never write must be zero in both
+    // buffers of each pair (see qp3d_adj_a_kernel)
     for (auto *p : S->L) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
+    for (auto *p : S->N) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
+    for (auto *p : S->Cf) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
     for (auto *p : S->g) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
 
     // ---- backward, one checkpoint segment at a time

@@ -1560,6 +1560,10 @@ __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
 // lambda * (d update / d m) are summed.  Pass B, per cell: the transposed
 // stencils of the six coefficient fields (second derivatives: the stencil
 // itself; first derivatives: its negative), zero outside the volume.
+// Pass A writes only what a cell can make non-zero (PML state and first-
+// derivative fields at PML cells, u_prev and second-derivative fields at
+// updated cells); the caller zeroes every buffer once, so the entries never
+// written stay zero in both buffers of each pair.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
 {
@@ -1630,11 +1634,18 @@ __global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
             else { c[5] += cn; c[2] += c1; c[3] += ct; c[4] += ct; }
         }
     }
-    a.Nu[i] = nu; a.Nup[i] = nup;
-    a.Nw1[i] = nw1; a.Nw1o[i] = nw1o; a.Np[i] = np_; a.Npo[i] = npo;
-    a.Nw21[i] = nw21; a.Nw3[i] = nw3; a.Nw3o[i] = nw3o;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) a.C[j][i] = c[j];
+    a.Nu[i] = nu;
+    if (!upd) return;
+    const bool in_pml = x < pml || x >= nx - pml || y < pml || y >= ny - pml || z < pml ||
+                        z >= nz - pml;
+    if (in_pml) {
+        a.Nw1[i] = nw1; a.Nw1o[i] = nw1o; a.Np[i] = np_; a.Npo[i] = npo;
+        a.Nw21[i] = nw21; a.Nw3[i] = nw3; a.Nw3o[i] = nw3o;
+        a.C[0][i] = c[0]; a.C[1][i] = c[1]; a.C[2][i] = c[2];
+    } else {
+        a.Nup[i] = nup;
+    }
+    a.C[3][i] = c[3]; a.C[4][i] = c[4]; a.C[5][i] = c[5];
 }
 
 __global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
