@@ -83,6 +83,8 @@ def parse():
     ap.add_argument("--workload", default="single",
                     choices=["single", "batch", "large", "adjoint"])
     ap.add_argument("--shots", type=int, default=64, help="batch workload: shots")
+    ap.add_argument("--spec-delta-ppm", type=int, default=None,
+                    help="smallest half-width of the predicted max window (ppm)")
     return ap.parse_args()
 
 
@@ -420,6 +422,8 @@ def run_batch_arm(args, dist):
     cells = [s.N for s in shots]
     work = sum(c * nt for c in cells)
     ctx = qp3d.Context(dist.local)
+    if args.spec_delta_ppm is not None:
+        ctx.tune(spec_delta_ppm=args.spec_delta_ppm)
     records = [np.empty((s.nt, s.hx, s.hy), np.float32) for s in shots]
     for _ in range(args.warmup):
         ctx.batch(shots, records)

@@ -854,7 +854,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "chunks") && value >= 0) ctx->tune_chunks = value;
     else if (!strcmp(key, "threshold_mode") && (value == 0 || value == 1)) ctx->threshold_mode = value;
     else if (!strcmp(key, "spec_delta_ppm") && value >= 0 && value <= 250000)
-        ctx->delta_min = value * 1e-6f;
+        ctx->delta_min = value * 1e-6f, ctx->delta_min_set = true;
     else if (!strcmp(key, "batch_graph") && (value == 0 || value == 1)) ctx->batch_graph = value;
     else if (!strcmp(key, "batch_tune") && (value == 0 || value == 1)) ctx->batch_tune = value;
     else if (!strcmp(key, "batch_candidate") && value >= -1 && value < 16)

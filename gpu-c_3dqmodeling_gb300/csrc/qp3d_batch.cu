@@ -330,7 +330,7 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
         d.nx = P.g.nx; d.ny = P.g.ny; d.nz = P.g.nz; d.ldy = P.ldy; d.pml = P.g.pml;
         d.sz = P.g.sz; d.nt = P.g.nt; d.hx = P.hx; d.hy = P.hy; d.plane = P.plane;
         d.dt = P.g.dt;
-        d.delta_min = ctx->delta_min;
+        d.delta_min = ctx->delta_min_set ? ctx->delta_min : 0.02f;
         d.nsrc = (int)P.src.size();
         d.spec_bias = ctx->spec_bias;
         d.err = ctx->errword;

@@ -77,7 +77,12 @@ struct qp3d_ctx {
     // tuning
     int gradmax_variant = 0, tune_tile_x = 0, tune_chunks = 0;
     int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
-    float delta_min = 0.01f;         // smallest half-width of the predicted window
+    // smallest half-width of the predicted window: 1% for single shots, 2% for
+    // batched ones (their small grids make the max jumpier: measured on 64
+    // config-3 shots 3417 exact re-runs at 1%, 1013 at 2%, 1.7% faster) unless
+    // set with "spec_delta_ppm"
+    float delta_min = 0.01f;
+    bool delta_min_set = false;
     float spec_bias = 0.0f;          // test hook: shifts the predicted window
     int param_fp16 = 0;              // store vp, eps, delta as IEEE half (next load)
     long long launches = 0;          // kernels launched by this context

@@ -203,8 +203,9 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * 1: register queue), "tile_x" (rows per tile, 0 = automatic),
  * "chunks" (z chunks, 0 = automatic), "threshold_mode" (0: gradmax pre-pass
  * every step, 1: speculative threshold), "spec_delta_ppm" (smallest
- * half-width of the predicted max window), "alt_cap" (deferred-cell list
- * entries, 0 = automatic).  Single shots: takes effect at the next
+ * half-width of the predicted max window; default 1% for single shots, 2% in
+ * qp3d_batch), "spec_bias_ppm" (test hook: shifts the predicted window so that
+ * predictions miss and steps re-run).  Single shots: takes effect at the next
  * qp3d_shot_load, or immediately for the loaded shot.  qp3d_batch:
  * "batch_graph" (1: replay steps from a captured graph), "batch_tune"
  * (1: time the candidate shapes), "batch_candidate" (shape index used when
