@@ -46,7 +46,7 @@ struct qp3d_ctx {
     float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21[2] = {};
     float *record = nullptr;
     float *gmax = nullptr;
-    // speculative threshold: per-step window, re-run flags, alternatives
+    // speculative threshold: per-step window, re-run flags, deferred-cell counts
     float *win = nullptr;
     int *redo = nullptr;
     unsigned *alt_count = nullptr;

@@ -188,8 +188,6 @@ cudaError_t launch_threshold(const float *gmax_k, float *T2, cudaStream_t stream
 cudaError_t launch_to_bf16(const float *a, __nv_bfloat16 *h, long long n, cudaStream_t stream);
 cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cudaStream_t stream);
 
-struct Shot;   // host-side, defined in qp3d_api.cu
-
 // Launchers (qp3d_kernels.cu).  All enqueue on `stream` and return the
 // launch error.
 cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p,

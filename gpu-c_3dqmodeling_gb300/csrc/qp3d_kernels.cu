@@ -2,21 +2,28 @@
 //
 // One time step of the reference (3dPureqPModeling_single_shot.cu:282-320:
 // grad -> D2H + host absMaxval -> scalar_operator -> wavefield_update ->
-// addsource -> exchange -> D2H + record crop) becomes two kernels:
+// addsource -> exchange -> D2H + record crop) becomes:
 //
-//   qp3d_gradmax_kernel   max over [5,n-5)^3 of |du/dx|,|du/dy|,|du/dz| of
-//                         u(k) (GPU_kernel.cu:14-33 + CPU_function.c:10-22),
-//                         reduced on the device with atomicMax on the float
-//                         bits (all values are >= 0, so the bit order is the
-//                         value order).
-//   qp3d_step_kernel      everything else in one pass: gradient, scalar
-//                         operator S (GPU_kernel.cu:87-115), Laplacians,
-//                         interior leapfrog and the six split-field PML faces
+//   qp3d_step_kernel      everything in one pass: gradient, scalar operator S
+//                         (GPU_kernel.cu:87-115), Laplacians, interior
+//                         leapfrog and the six split-field PML faces
 //                         (GPU_kernel.cu:534-639), source injection
-//                         (GPU_kernel.cu:720-731) and the receiver plane
-//                         (3dPureqPModeling_single_shot.cu:333-337).  The
-//                         time-level rotation (GPU_kernel.cu:733-812) is done
-//                         by the host swapping buffer indices.
+//                         (GPU_kernel.cu:720-731), the receiver plane
+//                         (3dPureqPModeling_single_shot.cu:333-337), and the
+//                         step's own max|grad u| (atomicMax on the float bits:
+//                         all values are >= 0, so bit order is value order).
+//                         The time-level rotation (GPU_kernel.cu:733-812) is
+//                         done by the host swapping buffer indices.
+//   the threshold         S needs the max of the step before any cell is
+//                         updated: either qp3d_gradmax_kernel computes it
+//                         first (GPU_kernel.cu:14-33 + CPU_function.c:10-22),
+//                         or the step runs speculatively with a predicted
+//                         window and qp3d_resolve / compact / fixup_kernel
+//                         settle the cells whose decision waited (a gated
+//                         exact re-run when the prediction missed).
+//
+// The same tile bodies run in the batched persistent kernels (many shots per
+// launch), and the adjoint kernels at the end of the file transpose the step.
 //
 // Both kernels march along z.  A CTA owns a tile of tile_x rows (x) by 32
 // cells (y) and a chunk of z planes.  Each thread owns one row and four
@@ -173,23 +180,6 @@ __device__ float threshold_m2(float gmax)
         x = n;
     }
     return x;
-}
-
-// ---------------------------------------------------------------------------
-// Region of a cell: -1 interior, else the PML face by the reference priority
-// left, right, forward, backward, top, bottom (GPU_kernel.cu:558-626).
-// ---------------------------------------------------------------------------
-enum { F_L = 0, F_R, F_F, F_BK, F_T, F_BO };
-
-__device__ __forceinline__ int region_of(int x, int y, int z, int nx, int ny, int nz, int pml)
-{
-    if (x < pml) return F_L;
-    if (x >= nx - pml) return F_R;
-    if (y < pml) return F_F;
-    if (y >= ny - pml) return F_BK;
-    if (z < pml) return F_T;
-    if (z >= nz - pml) return F_BO;
-    return -1;
 }
 
 // ---------------------------------------------------------------------------
@@ -756,12 +746,13 @@ __device__ __forceinline__ void cell_face(int fx, int lix, int fy, int liy, int 
 //   SPEC = true: the max of the step is not known yet.  It is predicted from
 //     the two previous steps with a window [M_lo, M_hi]; a cell whose m2 lies
 //     in (T2(M_lo), T2(M_hi)] has an uncertain decision: the kernel computes
-//     it as "above" and appends (cell, m2) to a list, and reduces the true max
-//     of the step into gmax[step] on the way.  qp3d_fixup_kernel then
-//     recomputes the listed cells that turn out to be below the threshold,
-//     or asks for the exact re-run when the max fell outside the window or
-//     the list overflowed.  The step never overwrites its inputs, so both
-//     are possible.  Both modes write bit-identical results.
+//     it as "above", marks it in the deferred-cell bitmask with its m2 and
+//     S = 1 value, and reduces the true max of the step into gmax[step] on
+//     the way.  The resolution, compaction and fix-up kernels then give the
+//     S = 1 result to the marked cells that turn out to be below the
+//     threshold, or ask for the exact re-run when the max fell outside the
+//     window.  The step never overwrites its inputs, so both are possible.
+//     Both modes write bit-identical results.
 // ---------------------------------------------------------------------------
 __device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &pred)
 {

@@ -428,7 +428,7 @@ class Context:
         return out
 
     def stats(self, k0=0, n=None):
-        """(redo flags, alternatives count) per step."""
+        """(re-run flags, deferred-cell counts) per step."""
         if n is None:
             n = self.step - k0
         redo = np.zeros(n, np.int32)
