@@ -45,8 +45,9 @@ struct AdjState {
     float *L[9] = {}, *N[9] = {}, *Cf[6] = {}, *g[3] = {};
     float *seg = nullptr;          // C volumes: u^k of the segment
     void *ck = nullptr;            // nck checkpoints x 9 volumes
-    float *resid = nullptr;        // nt * hx * hy
-    float *T2 = nullptr;
+    float *resid = nullptr;        // nt * hx * hy: d_obs, then the residual
+    float *T2 = nullptr;           // thresholds of a segment
+    double *misfit = nullptr;
 };
 
 void adjoint_free(AdjState *s)
@@ -60,6 +61,7 @@ void adjoint_free(AdjState *s)
     cudaFree(s->ck);
     cudaFree(s->resid);
     cudaFree(s->T2);
+    cudaFree(s->misfit);
     delete s;
 }
 
@@ -96,7 +98,8 @@ int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, size_t rec
                                               : 9 * sizeof(float));
     CK(cudaMalloc(&s->ck, per * nck));
     CK(cudaMalloc(&s->resid, rec * sizeof(float)));
-    CK(cudaMalloc(&s->T2, sizeof(float)));
+    CK(cudaMalloc(&s->T2, sizeof(float) * C));
+    CK(cudaMalloc(&s->misfit, sizeof(double)));
     s->C = C;
     s->nck = nck;
     s->bf16 = bf16;
@@ -163,17 +166,13 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
         }
         if ((rc = qp3d_internal_enqueue_step(ctx))) return rc;
     }
-    // ---- residual and misfit
-    std::vector<float> r(rec);
-    if ((rc = qp3d_shot_read_record(ctx, 0, nt, r.data()))) return rc;
-    double J = 0.0;
-    for (size_t i = 0; i < rec; ++i) {
-        r[i] -= d_obs[i];
-        J += 0.5 * (double)r[i] * r[i];
-    }
-    if (misfit) *misfit = J;
-    CK(cudaMemcpyAsync(S->resid, r.data(), rec * sizeof(float), cudaMemcpyHostToDevice,
+    // ---- residual and misfit, on the device
+    CK(cudaMemcpyAsync(S->resid, d_obs, rec * sizeof(float), cudaMemcpyHostToDevice,
                        ctx->stream));
+    CK(cudaMemsetAsync(S->misfit, 0, sizeof(double), ctx->stream));
+    CKL(launch_residual(ctx->record, S->resid, S->resid, (long long)rec, S->misfit, ctx->stream));
+    double J = 0.0;
+    CK(cudaMemcpyAsync(&J, S->misfit, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     // every entry the adjoint kernels never write must be zero in both
     // buffers of each pair (see qp3d_adj_a_kernel)
     for (auto *p : S->L) CK(cudaMemsetAsync(p, 0, vb, ctx->stream));
@@ -186,7 +185,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     memset(&a, 0, sizeof(a));
     a.nx = g->nx; a.ny = g->ny; a.nz = g->nz; a.ldy = ctx->ldy; a.pml = g->pml; a.sz = g->sz;
     a.hx = ctx->hx; a.hy = ctx->hy; a.plane = ctx->plane; a.k = ctx->coefs; a.dt = g->dt;
-    a.K = ctx->K; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers; a.T2 = S->T2;
+    a.K = ctx->K; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers;
     for (int c = nck - 1; c >= 0; --c) {
         const int k0 = c * C, k1 = std::min(nt, k0 + C);
         if ((rc = qp3d_internal_restore_step(ctx, k0))) return rc;
@@ -205,8 +204,9 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
                                cudaMemcpyDeviceToDevice, ctx->stream));
             if ((rc = qp3d_internal_enqueue_step(ctx))) return rc;
         }
+        CKL(launch_threshold(ctx->gmax + k0, S->T2, k1 - k0, ctx->stream));
         for (int k = k1 - 1; k >= k0; --k) {
-            CKL(launch_threshold(ctx->gmax + k, S->T2, ctx->stream));
+            a.T2 = S->T2 + (k - k0);
             a.u = S->seg + (size_t)(k - k0) * vol;
             a.resid = S->resid + (size_t)k * ctx->hx * ctx->hy;
             const float **Lc[9] = {&a.Lu, &a.Lup, &a.Lw1, &a.Lw1o, &a.Lp, &a.Lpo, &a.Lw21,
@@ -243,5 +243,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
                     outs[q][i] += gi;
                 }
     }
-    return qp3d_shot_sync(ctx);
+    rc = qp3d_shot_sync(ctx);
+    if (!rc && misfit) *misfit = J;
+    return rc;
 }

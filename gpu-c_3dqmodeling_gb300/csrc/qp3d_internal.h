@@ -184,7 +184,9 @@ struct AdjParams {
 };
 
 cudaError_t launch_adjoint_step(const AdjParams &a, cudaStream_t stream);
-cudaError_t launch_threshold(const float *gmax_k, float *T2, cudaStream_t stream);
+cudaError_t launch_threshold(const float *gmax, float *T2, int n, cudaStream_t stream);
+cudaError_t launch_residual(const float *rec, const float *dobs, float *r, long long n,
+                            double *misfit, cudaStream_t stream);
 cudaError_t launch_to_bf16(const float *a, __nv_bfloat16 *h, long long n, cudaStream_t stream);
 cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cudaStream_t stream);
 

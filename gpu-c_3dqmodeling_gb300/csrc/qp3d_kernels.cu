@@ -1664,9 +1664,33 @@ __global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
     a.Nu[i] += acc;
 }
 
-__global__ void qp3d_threshold_kernel(const float *gmax_k, float *T2)
+__global__ void qp3d_threshold_kernel(const float *gmax, float *T2, int n)
 {
-    if (threadIdx.x == 0) *T2 = threshold_m2(*gmax_k);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) T2[i] = threshold_m2(gmax[i]);
+}
+
+// Record residual r = record - d_obs and the misfit 1/2 sum r^2 (FP64, one
+// atomic per block).
+__global__ void qp3d_residual_kernel(const float *rec, const float *dobs, float *r, long long n,
+                                     double *misfit)
+{
+    __shared__ double s[32];
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float v = rec[i] - dobs[i];
+        r[i] = v;
+        acc += 0.5 * (double)v * (double)v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        atomicAdd(misfit, t);
+    }
 }
 
 __global__ void qp3d_to_bf16_kernel(const float *a, __nv_bfloat16 *h, long long n)
@@ -1872,9 +1896,17 @@ cudaError_t launch_adjoint_step(const AdjParams &a, cudaStream_t stream)
     return cudaGetLastError();
 }
 
-cudaError_t launch_threshold(const float *gmax_k, float *T2, cudaStream_t stream)
+cudaError_t launch_threshold(const float *gmax, float *T2, int n, cudaStream_t stream)
 {
-    qp3d_threshold_kernel<<<1, 32, 0, stream>>>(gmax_k, T2);
+    qp3d_threshold_kernel<<<1, 256, 0, stream>>>(gmax, T2, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_residual(const float *rec, const float *dobs, float *r, long long n,
+                            double *misfit, cudaStream_t stream)
+{
+    long long b = (n + 255) / 256;
+    qp3d_residual_kernel<<<(int)(b > 4096 ? 4096 : b), 256, 0, stream>>>(rec, dobs, r, n, misfit);
     return cudaGetLastError();
 }
 
