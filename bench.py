@@ -236,6 +236,7 @@ def cpu_sample(shot, nsteps, k0=1500, seed=0):
     st.u2[:] = u_cur
     st.pml[:] = pml
     threads = os.cpu_count() or 1
+    k0 = max(0, min(k0, shot.nt - nsteps))   # the wavelet has nt samples
     t0 = time.perf_counter()
     O.run(O.REF32, prob, k0=k0, nsteps=nsteps, state=st, nthreads=threads, want_record=False)
     return time.perf_counter() - t0, threads
