@@ -82,7 +82,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="single",
                     choices=["single", "batch", "large", "adjoint"])
-    ap.add_argument("--shots", type=int, default=64, help="batch workload: shots")
+    ap.add_argument("--shots", type=int, default=64,
+                    help="batch workload: shots; adjoint workload: up to 16 (a square grid)")
     ap.add_argument("--spec-delta-ppm", type=int, default=None,
                     help="smallest half-width of the predicted max window (ppm)")
     return ap.parse_args()
@@ -579,7 +580,8 @@ def run_adjoint_arm(args, dist):
     import qp3d
     import synthetic
     nt = args.nt if args.nt is not None else 2000
-    true, start = synthetic.adjoint_case(nt=nt)
+    grid = 4 if args.shots >= 16 else max(1, int(round(args.shots ** 0.5)))   # grid x grid shots
+    true, start = synthetic.adjoint_case(nt=nt, grid=grid)
     ctx = qp3d.Context(dist.local)
     d_obs = [ctx.forward(s).copy() for s in true]
     N = start[0].N
