@@ -37,7 +37,9 @@ Nz0 in [128, 200], 20-cell PML, 10.8 M padded cells on average) cut from one
 smoothed by a 3D Gaussian of 5 cells, 16 shots on a 4x4 surface grid, 2000
 steps, sqrt(nt) checkpoints in FP32 (and with BF16 PML levels beside it);
 value = seconds per shot of the gradient (forward, residual, checkpointed
-backward), the records of the true model made first.
+backward), the records of the true model made first.  Beside it, the schedule
+that keeps every u^k in device memory (88 GB here, no recomputation; the
+library's default when it fits), whose gradient is identical.
 
 --workload large measures the large mixed-precision configuration (one bench
 step = one shot): 800x800x400 cells + 40-cell PML (880x880x480 padded, 372 M
@@ -590,8 +592,9 @@ def run_adjoint_arm(args, dist):
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
     clocks = Clocks(gpu_index)
     launches0 = ctx.launch_count()
-    for name, bf16 in (("fp32_checkpoints", 0), ("bf16_pml_checkpoints", 1)):
-        ctx.tune(adj_ckpt_bf16=bf16)
+    for name, bf16, keep in (("fp32_checkpoints", 0, 0), ("bf16_pml_checkpoints", 1, 0),
+                             ("keep_all", 0, 1)):
+        ctx.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
         for _ in range(args.warmup):
             ctx.adjoint(start[0], d_obs[0])
         grads = [np.zeros(N, np.float64) for _ in range(3)]
@@ -610,6 +613,8 @@ def run_adjoint_arm(args, dist):
     for i, p in enumerate(("vp", "eps", "delta")):
         a, b = res["bf16_pml_checkpoints"]["grads"][i], res["fp32_checkpoints"]["grads"][i]
         cos[p] = round(float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b))), 6)
+    keep_same = all(np.array_equal(a, b) for a, b in zip(res["keep_all"]["grads"],
+                                                          res["fp32_checkpoints"]["grads"]))
     t_fwd = None
     ctx.load(start[0])
     tot, _, _ = ctx.time(nt, per_kernel=False)
@@ -627,6 +632,8 @@ def run_adjoint_arm(args, dist):
                        "grid": [start[0].nx, start[0].ny, start[0].nz], "nt": nt,
                        "parallelism": "single"},
             "bf16_pml_checkpoints_s_per_shot": res["bf16_pml_checkpoints"]["s_per_shot"],
+            "keep_all_s_per_shot": res["keep_all"]["s_per_shot"],
+            "keep_all_gradient_identical": keep_same,
             "forward_only_s_per_shot": round(t_fwd, 4),
             "misfit": res["fp32_checkpoints"]["misfit"],
             "cosine_bf16_pml_vs_fp32_checkpoints": cos,

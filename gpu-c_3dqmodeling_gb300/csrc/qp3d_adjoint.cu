@@ -9,11 +9,15 @@
 // (oracle/qp3d_adjoint.c) implements the same operator and passes
 // dot-product and finite-difference tests.
 //
-// Schedule: the forward pass stores the state every C = ceil(sqrt(nt)) steps
-// (nine volumes: u, u_prev and the seven live PML levels), in FP32 by default
-// so that the recomputation is bit-identical to the forward; the backward
-// pass restores each checkpoint, recomputes its C steps keeping u^k, and runs
-// the C adjoint steps backward.  With "adj_ckpt_bf16" the PML levels are kept
+// Schedule: the adjoint step reads u^k (S and its derivatives) and nothing
+// else of the forward state.  When the nt wavefields fit in device memory
+// (240x240x190 padded cells x 2000 steps is 88 GB) the forward pass keeps
+// every u^k and the backward pass runs straight through.  Otherwise the
+// forward pass stores the state every C = ceil(sqrt(nt)) steps (nine volumes:
+// u, u_prev and the seven live PML levels), in FP32 by default so that the
+// recomputation is bit-identical to the forward; the backward pass restores
+// each checkpoint, recomputes its C steps keeping u^k, and runs the C adjoint
+// steps backward.  With "adj_ckpt_bf16" the PML levels are kept
 // in BF16 (22 instead of 36 bytes per cell and checkpoint); u always stays
 // FP32 because S depends on the direction of grad u, a difference of
 // neighbouring values that BF16 rounding of a smooth wavefield destroys.  The
@@ -22,7 +26,7 @@
 // wavefield (measured on 16 shots of 240x240x190: cosine against FP32
 // checkpoints 0.999999 vp, 0.99997 eps, 0.91 delta with BF16 PML levels,
 // 0.87 delta with an all-BF16 state).  Device memory:
-// ~27 + C volumes plus the checkpoints.  Gradients are summed per shot in
+// ~27 volumes plus nt (all kept) or C volumes and the checkpoints.  Gradients are summed per shot in
 // FP32 on the device and added to the caller's FP64 arrays.
 #include "qp3d_ctx.h"
 
@@ -41,9 +45,9 @@ namespace qp3d {
 
 struct AdjState {
     long long vol = 0;
-    int nt = 0, C = 0, nck = 0, bf16 = 1;
+    int nt = 0, C = 0, nck = 0, bf16 = 1, keep = 0;
     float *L[9] = {}, *N[9] = {}, *Cf[6] = {}, *g[3] = {};
-    float *seg = nullptr;          // C volumes: u^k of the segment
+    float *seg = nullptr;          // C volumes: u^k of the segment (keep: C = nt)
     void *ck = nullptr;            // nck checkpoints x 9 volumes
     float *resid = nullptr;        // nt * hx * hy: d_obs, then the residual
     float *T2 = nullptr;           // thresholds of a segment
@@ -84,7 +88,7 @@ void live_state(qp3d_ctx *ctx, int k, float *v[9])
     v[8] = ctx->W3[k % 3];
 }
 
-int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, size_t rec)
+int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, int keep, size_t rec)
 {
     const size_t vb = (size_t)s->vol * sizeof(float);
     for (int i = 0; i < 9; ++i) {
@@ -96,13 +100,14 @@ int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, size_t rec
     CK(cudaMalloc(&s->seg, vb * C));
     const size_t per = (size_t)s->vol * (bf16 ? 2 * sizeof(float) + 7 * sizeof(__nv_bfloat16)
                                               : 9 * sizeof(float));
-    CK(cudaMalloc(&s->ck, per * nck));
+    if (nck) CK(cudaMalloc(&s->ck, per * nck));
     CK(cudaMalloc(&s->resid, rec * sizeof(float)));
     CK(cudaMalloc(&s->T2, sizeof(float) * C));
     CK(cudaMalloc(&s->misfit, sizeof(double)));
     s->C = C;
     s->nck = nck;
     s->bf16 = bf16;
+    s->keep = keep;
     return QP3D_OK;
 }
 
@@ -123,26 +128,35 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     const int nt = g->nt;
     const long long vol = ctx->vol;
     const size_t rec = (size_t)nt * ctx->hx * ctx->hy;
-    const int C = std::max(1, (int)std::ceil(std::sqrt((double)std::max(nt, 1))));
-    const int nck = (nt + C - 1) / C;
-    // state buffers, reused when the geometry repeats
+    const size_t vb = (size_t)vol * sizeof(float);
+    // state buffers, reused when the geometry and the schedule repeat
     AdjState *&S = ctx->adj;
-    if (S && (S->vol != vol || S->nt != nt || S->bf16 != ctx->adj_bf16)) {
+    if (S && (S->vol != vol || S->nt != nt || S->bf16 != ctx->adj_bf16 ||
+              (ctx->adj_keep >= 0 && S->keep != ctx->adj_keep))) {
         adjoint_free(S);
         S = nullptr;
     }
+    int keep = S ? S->keep : ctx->adj_keep;
+    if (keep < 0) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        const size_t need = (size_t)nt * vb + 32 * vb + rec * sizeof(float);
+        keep = fr > need + (8ull << 30) ? 1 : 0;
+    }
+    const int C = keep ? std::max(nt, 1)
+                       : std::max(1, (int)std::ceil(std::sqrt((double)std::max(nt, 1))));
+    const int nck = keep ? 0 : (nt + C - 1) / C;
     if (!S) {
         S = new (std::nothrow) AdjState();
         if (!S) return ctx_fail(ctx, QP3D_ERR_NOMEM, "out of host memory");
         S->vol = vol;
         S->nt = nt;
-        if ((rc = alloc_state(ctx, S, C, nck, ctx->adj_bf16, rec))) {
+        if ((rc = alloc_state(ctx, S, C, nck, ctx->adj_bf16, keep, rec))) {
             adjoint_free(S);
             S = nullptr;
             return rc;
         }
     }
-    const size_t vb = (size_t)vol * sizeof(float);
     // checkpoint c: volumes 0, 1 (u, u_prev) FP32, 2..8 FP32 or BF16
     const size_t hb = S->bf16 ? (size_t)vol * sizeof(__nv_bfloat16) : vb;
     auto ck_slot = [&](int c, int j) {
@@ -150,9 +164,12 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
                (j < 2 ? (size_t)j * vb : 2 * vb + (size_t)(j - 2) * hb);
     };
 
-    // ---- forward with checkpoints
+    // ---- forward, keeping u^k or checkpoints
     for (int k = 0; k < nt; ++k) {
-        if (k % C == 0) {
+        if (keep) {
+            CK(cudaMemcpyAsync(S->seg + (size_t)k * vol, ctx->U[ctx->cur], vb,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+        } else if (k % C == 0) {
             float *v[9];
             live_state(ctx, k, v);
             for (int j = 0; j < 9; ++j) {
@@ -186,23 +203,26 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     a.nx = g->nx; a.ny = g->ny; a.nz = g->nz; a.ldy = ctx->ldy; a.pml = g->pml; a.sz = g->sz;
     a.hx = ctx->hx; a.hy = ctx->hy; a.plane = ctx->plane; a.k = ctx->coefs; a.dt = g->dt;
     a.K = ctx->K; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers;
-    for (int c = nck - 1; c >= 0; --c) {
+    for (int c = (keep ? 1 : nck) - 1; c >= 0; --c) {
         const int k0 = c * C, k1 = std::min(nt, k0 + C);
-        if ((rc = qp3d_internal_restore_step(ctx, k0))) return rc;
-        float *v[9];
-        live_state(ctx, k0, v);
-        for (int j = 0; j < 9; ++j) {
-            if (S->bf16 && j >= 2)
-                CKL(launch_from_bf16(reinterpret_cast<const __nv_bfloat16 *>(ck_slot(c, j)), v[j],
-                                     vol, ctx->stream));
-            else
-                CK(cudaMemcpyAsync(v[j], ck_slot(c, j), vb, cudaMemcpyDeviceToDevice,
-                                   ctx->stream));
-        }
-        for (int k = k0; k < k1; ++k) {
-            CK(cudaMemcpyAsync(S->seg + (size_t)(k - k0) * vol, ctx->U[ctx->cur], vb,
-                               cudaMemcpyDeviceToDevice, ctx->stream));
-            if ((rc = qp3d_internal_enqueue_step(ctx))) return rc;
+        if (!keep) {   // restore the checkpoint, recompute keeping u^k
+            if ((rc = qp3d_internal_restore_step(ctx, k0))) return rc;
+            float *v[9];
+            live_state(ctx, k0, v);
+            for (int j = 0; j < 9; ++j) {
+                if (S->bf16 && j >= 2)
+                    CKL(launch_from_bf16(
+                        reinterpret_cast<const __nv_bfloat16 *>(ck_slot(c, j)), v[j], vol,
+                        ctx->stream));
+                else
+                    CK(cudaMemcpyAsync(v[j], ck_slot(c, j), vb, cudaMemcpyDeviceToDevice,
+                                       ctx->stream));
+            }
+            for (int k = k0; k < k1; ++k) {
+                CK(cudaMemcpyAsync(S->seg + (size_t)(k - k0) * vol, ctx->U[ctx->cur], vb,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+                if ((rc = qp3d_internal_enqueue_step(ctx))) return rc;
+            }
         }
         CKL(launch_threshold(ctx->gmax + k0, S->T2, k1 - k0, ctx->stream));
         for (int k = k1 - 1; k >= k0; --k) {

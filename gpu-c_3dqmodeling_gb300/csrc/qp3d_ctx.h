@@ -95,6 +95,7 @@ struct qp3d_ctx {
     // adjoint (qp3d_adjoint)
     qp3d::AdjState *adj = nullptr;
     int adj_bf16 = 0;                // 1: PML levels of the checkpoints in BF16
+    int adj_keep = -1;               // 1: keep every u^k, 0: checkpoints, -1: by free memory
 };
 inline int ctx_fail(qp3d_ctx *c, int code, const char *fmt, ...)
 {

@@ -1639,14 +1639,35 @@ __global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
     a.C[3][i] = c[3]; a.C[4][i] = c[4]; a.C[5][i] = c[5];
 }
 
+// Pass B: Nu += the transposed stencils of the six coefficient fields.
+// Outside the PML shell the first-derivative fields (Cx, Cy, Cz) are zero and
+// Cyy equals Cxx (qp3d_adj_a_kernel), so a block whose whole footprint (its
+// cells and 5 cells around them) lies inside reads two fields and no bounds.
 __global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
 {
-    const int y = blockIdx.x * 32 + threadIdx.x, x = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+    const int y0 = blockIdx.x * 32, x0 = blockIdx.y * 8, z = blockIdx.z;
+    const int y = y0 + threadIdx.x, x = x0 + threadIdx.y;
     if (y >= a.ny || x >= a.nx) return;
     const long long i = (long long)z * a.plane + (long long)x * a.ldy + y;
+    const Coefs &k = a.k;
+    if (x0 - kRadius >= a.pml && x0 + 8 + kRadius <= a.nx - a.pml && y0 - kRadius >= a.pml &&
+        y0 + 32 + kRadius <= a.ny - a.pml && z - kRadius >= a.pml &&
+        z + kRadius < a.nz - a.pml) {
+        const float *H = a.C[3], *V = a.C[5];
+        const float h0 = H[i];
+        float acc = k.kx * h0 + k.ky * h0 + k.kz * V[i];
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m) {
+            const int d = m + 1;
+            const long long dx = (long long)d * a.ldy, dz = (long long)d * a.plane;
+            acc += k.c2x[m] * (H[i + dx] + H[i - dx]) + k.c2y[m] * (H[i + d] + H[i - d]) +
+                   k.c2z[m] * (V[i + dz] + V[i - dz]);
+        }
+        a.Nu[i] += acc;
+        return;
+    }
     const float *Cx = a.C[0], *Cy = a.C[1], *Cz = a.C[2], *Cxx = a.C[3], *Cyy = a.C[4],
                 *Czz = a.C[5];
-    const Coefs &k = a.k;
     float acc = k.kx * Cxx[i] + k.ky * Cyy[i] + k.kz * Czz[i];
 #pragma unroll
     for (int m = 0; m < kRadius; ++m) {

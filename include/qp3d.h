@@ -145,10 +145,14 @@ int qp3d_batch_get_stats(const qp3d_ctx *ctx, qp3d_batch_stats *out);
  * its scalar operator S frozen per step and cell (threshold decision and
  * unit normal of the forward wavefield; S's dependence on epsilon and delta
  * is differentiated); the adjoint is the exact transpose of that step,
- * split-field PML included.  Checkpoints every ceil(sqrt(nt)) steps, FP32 by
- * default (the recomputation is bit-identical to the forward);
+ * split-field PML included.  The backward pass needs u^k of every step: when
+ * all nt wavefields fit in device memory the forward keeps them
+ * ("adj_keep_all", default -1: decided by free memory), otherwise it stores
+ * checkpoints every ceil(sqrt(nt)) steps and the backward recomputes each
+ * segment, bit-identically with FP32 checkpoints (default);
  * "adj_ckpt_bf16" = 1 keeps the seven PML state levels in BF16 (u and u_prev
- * stay FP32), which perturbs mostly the delta gradient.  The gradient is added (+=) to the caller's padded [nz][nx][ny]
+ * stay FP32), which perturbs mostly the delta gradient.  Both schedules give
+ * the same gradient bit for bit with FP32 checkpoints.  The gradient is added (+=) to the caller's padded [nz][nx][ny]
  * FP64 arrays on the cells outside the PML shell (the shell's parameters
  * extend the interior edge and are held fixed); NULL skips one.  misfit:
  * out, J (may be NULL).  Needs FP32 parameter storage and sources and
@@ -215,7 +219,10 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * vp, epsilon and delta as IEEE half, rounded to nearest; the stencil stays
  * FP32, and the results equal an FP32 run on the rounded model bit for bit;
  * qp3d_batch always stores FP32).  "adj_ckpt_bf16" (qp3d_adjoint
- * checkpoint storage of the PML state, 0: FP32 (default), 1: BF16). */
+ * checkpoint storage of the PML state, 0: FP32 (default), 1: BF16).
+ * "adj_keep_all" (qp3d_adjoint schedule, 1: keep u^k of every step,
+ * 0: checkpoints and recomputation, -1: keep all when nt wavefields fit in
+ * the free device memory less 8 GiB). */
 int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
 int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
 
