@@ -45,6 +45,8 @@ library's default when it fits), whose gradient is identical.
 step = one shot): 800x800x400 cells + 40-cell PML (880x880x480 padded, 372 M
 cells), 20 dipping layers and 30 Gaussian velocity anomalies, 5000 steps,
 with vp/eps/delta stored as FP32 and as FP16 (param_fp16), wavefields FP32.
+The two full-size records are compared on every 10th step (rel-L2 and max
+abs / peak of FP16 against FP32).
 """
 import argparse
 import json
@@ -528,6 +530,7 @@ def run_large_arm(args, dist):
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
     peak, peak_kind = hbm_peak()
     runs = {}
+    rec_sample = {}
     launches0 = ctx.launch_count()
     clocks = Clocks(gpu_index)
     for name, fp16 in (("fp32_params", 0), ("fp16_params", 1)):
@@ -543,6 +546,9 @@ def run_large_arm(args, dist):
             t, s, _ = ctx.time(nt)
             tot += t
             ms_s += s
+        # every 10th record step of the full-size run, for the FP16 vs FP32
+        # comparison (outside the timed region)
+        rec_sample[name] = np.stack([ctx.record(k, 1)[0] for k in range(0, nt, 10)])
         bstep = algorithmic_bytes(shot, 2 if fp16 else 4)[0]
         t_step = ms_s / (nt * args.steps) / 1e3
         runs[name] = {"value": round(cells * nt * args.steps / (tot / 1e3) / 1e9, 3),
@@ -554,6 +560,20 @@ def run_large_arm(args, dist):
                                    "algorithmic_bytes_per_launch": bstep}}
     clk = clocks.stop()
     gpu_launches = ctx.launch_count() - launches0
+    a32, a16 = rec_sample["fp32_params"], rec_sample["fp16_params"]
+    num = den = 0.0
+    dmax = pmax = 0.0
+    for p32, p16 in zip(a32, a16):
+        d = p16.astype(np.float64) - p32
+        num += float(np.sum(d * d))
+        den += float(np.sum(p32.astype(np.float64) ** 2))
+        dmax = max(dmax, float(np.max(np.abs(d))))
+        pmax = max(pmax, float(np.max(np.abs(p32))))
+    fp16_vs_fp32 = {
+        "rel_l2": (num / den) ** 0.5 if den > 0 else None,
+        "max_abs_over_peak": dmax / pmax if pmax > 0 else None,
+        "sampled": "record planes of every 10th step (%d of %d), full %dx%d surface"
+                   % (a32.shape[0], nt, a32.shape[1], a32.shape[2])}
     if dist.rank == 0:
         line = {
             "metric": "Gcell-updates/s", "value": runs["fp16_params"]["value"], "unit": "Gcell/s",
@@ -565,6 +585,7 @@ def run_large_arm(args, dist):
                        "grid": [shot.nx, shot.ny, shot.nz], "cells": cells, "nt": nt,
                        "l2": "inputs larger than L2", "parallelism": "single"},
             "runs": runs,
+            "fp16_vs_fp32_record": fp16_vs_fp32,
             "gpu_launches": gpu_launches,
             "clocks": clk,
         }

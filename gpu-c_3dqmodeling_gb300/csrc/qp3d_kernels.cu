@@ -1555,6 +1555,12 @@ __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
 // derivative fields at PML cells, u_prev and second-derivative fields at
 // updated cells); the caller zeroes every buffer once, so the entries never
 // written stay zero in both buffers of each pair.
+// The gradient is checked against the FP64 adjoint by cosine, not bit for
+// bit, so these kernels take the cheaper arithmetic: fast division
+// (__fdividef, 2 ulp) in S and its derivatives, fused multiply-adds in the
+// transposed stencils.  Both passes are bound by the L1 load path and
+// instruction issue (31 and 63 gathered taps per cell); a shared-memory
+// z-marching form (register queue along z) was measured slower on GB300.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
 {
@@ -1579,13 +1585,14 @@ __global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
         const float h2 = fmaf(Uy, Uy, Ux * Ux), m2 = fmaf(Uz, Uz, h2);
         float S = 1.0f, dSe = 0.0f, dSd = 0.0f;
         if (m2 > *a.T2) {
-            const float aa = h2 / m2, bb = 1.0f - aa, D = fmaf(E2, aa, 1.0f);
-            const float ab8 = 8.0f * aa * bb / (D * D);
+            const float aa = __fdividef(h2, m2), bb = 1.0f - aa, D = fmaf(E2, aa, 1.0f);
+            const float iD = __fdividef(1.0f, D);
+            const float ab8 = 8.0f * aa * bb * iD * iD;
             const float q = 0.125f * R8 * ab8;
             const float r = sqrtf(fmaxf(1.0f - q, 0.0f));
             S = 0.5f + 0.5f * r;
-            const float dSdq = r > 0.0f ? -0.25f / r : 0.0f;
-            dSe = dSdq * ab8 * (1.0f - aa * R8 / (2.0f * D));
+            const float dSdq = r > 0.0f ? __fdividef(-0.25f, r) : 0.0f;
+            dSe = dSdq * ab8 * (1.0f - 0.5f * aa * R8 * iD);
             dSd = -dSdq * ab8;
         }
         const float KS = K * S;
@@ -1660,8 +1667,9 @@ __global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
         for (int m = 0; m < kRadius; ++m) {
             const int d = m + 1;
             const long long dx = (long long)d * a.ldy, dz = (long long)d * a.plane;
-            acc += k.c2x[m] * (H[i + dx] + H[i - dx]) + k.c2y[m] * (H[i + d] + H[i - d]) +
-                   k.c2z[m] * (V[i + dz] + V[i - dz]);
+            acc = fmaf(k.c2x[m], H[i + dx] + H[i - dx], acc);
+            acc = fmaf(k.c2y[m], H[i + d] + H[i - d], acc);
+            acc = fmaf(k.c2z[m], V[i + dz] + V[i - dz], acc);
         }
         a.Nu[i] += acc;
         return;
@@ -1679,8 +1687,12 @@ __global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
         if (y - d >= 0) { syy += Cyy[i - d]; sy += Cy[i - d]; }
         if (z + d < a.nz) { const long long j = i + (long long)d * a.plane; szz += Czz[j]; sz -= Cz[j]; }
         if (z - d >= 0) { const long long j = i - (long long)d * a.plane; szz += Czz[j]; sz += Cz[j]; }
-        acc += k.c2x[m] * sxx + k.c2y[m] * syy + k.c2z[m] * szz + k.cx[m] * sx + k.cy[m] * sy +
-               k.cz[m] * sz;
+        acc = fmaf(k.c2x[m], sxx, acc);
+        acc = fmaf(k.c2y[m], syy, acc);
+        acc = fmaf(k.c2z[m], szz, acc);
+        acc = fmaf(k.cx[m], sx, acc);
+        acc = fmaf(k.cy[m], sy, acc);
+        acc = fmaf(k.cz[m], sz, acc);
     }
     a.Nu[i] += acc;
 }
