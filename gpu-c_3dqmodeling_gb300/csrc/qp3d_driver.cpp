@@ -8,12 +8,15 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace qp3d {
 int write_snapshot_files(void *user, int step, int kind, const float *data, int n0, int n1,
                          int n2);
+std::string snapshot_file_name(const std::string &prefix, int kind, int step);
 }
 
 namespace {
@@ -119,19 +122,61 @@ void shot_geom_model(const qp3d_parameters &P, ShotInputs &in, const float *c, c
     m.c = c; m.c2 = c2;
 }
 
+// RSF header of a file of [n_k]...[n_1] floats, axes given fastest first.
+int rsf(const char *file, std::initializer_list<std::pair<long long, float>> ax,
+        std::initializer_list<const char *> labels)
+{
+    long long n[4];
+    float d[4];
+    const char *lab[4];
+    int k = 0;
+    for (const auto &a : ax) n[k] = a.first, d[k] = a.second, ++k;
+    k = 0;
+    for (const char *l : labels) lab[k++] = l;
+    return qp3d_write_rsf_header(file, (int)ax.size(), n, d, lab);
+}
+
+// Snapshot callback: the files of write_snapshot_files, plus their RSF
+// headers when asked for.
+struct SnapFiles {
+    std::string prefix;
+    bool rsf;
+    float dx, dy, dz;
+};
+
+int snapshot_with_headers(void *user, int step, int kind, const float *data, int n0, int n1,
+                          int n2)
+{
+    const SnapFiles *s = static_cast<const SnapFiles *>(user);
+    std::string prefix = s->prefix;
+    if (qp3d::write_snapshot_files(&prefix, step, kind, data, n0, n1, n2)) return -1;
+    if (!s->rsf) return 0;
+    const std::string name = qp3d::snapshot_file_name(s->prefix, kind, step);
+    switch (kind) {
+    case QP3D_SNAP_VOLUME:   // [z][x][y]
+        return rsf(name.c_str(), {{n2, s->dy}, {n1, s->dx}, {n0, s->dz}}, {"y", "x", "z"});
+    case QP3D_SNAP_XZ:       // [z][x]
+        return rsf(name.c_str(), {{n1, s->dx}, {n0, s->dz}}, {"x", "z"});
+    case QP3D_SNAP_YZ:       // [z][y]
+        return rsf(name.c_str(), {{n1, s->dy}, {n0, s->dz}}, {"y", "z"});
+    default:                 // [x][y]
+        return rsf(name.c_str(), {{n1, s->dy}, {n0, s->dx}}, {"y", "x"});
+    }
+}
+
 int model_shot(qp3d_ctx *ctx, const qp3d_parameters &P, ShotInputs &in, const float *c,
-               const float *c2, int snapflag, const char *snap_prefix, float *record, char *err,
-               size_t errlen)
+               const float *c2, int snapflag, const char *snap_prefix, bool write_rsf,
+               float *record, char *err, size_t errlen)
 {
     qp3d_geom g;
     qp3d_model m;
     shot_geom_model(P, in, c, c2, g, m);
-    std::string prefix(snap_prefix);
+    SnapFiles files{std::string(snap_prefix), write_rsf, P.dx, P.dy, P.dz};
     qp3d_snap snap;
     snap.ntsnap = P.ntsnap;
     snap.kinds = 0xFu;
-    snap.fn = qp3d::write_snapshot_files;
-    snap.user = &prefix;
+    snap.fn = snapshot_with_headers;
+    snap.user = &files;
     int rc = qp3d_forward(ctx, &g, &m, record, (snapflag == 1 && P.ntsnap > 0) ? &snap : nullptr);
     if (rc) return fail(err, errlen, rc, "modeling failed: %s", qp3d_ctx_last_error(ctx));
     return QP3D_OK;
@@ -183,7 +228,7 @@ extern "C" int qp3d_parse_parameter_file(const char *path, qp3d_parameters *P, c
 extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options *opt, char *err,
                                        size_t errlen)
 {
-    qp3d_run_options o{0, QP3D_DIRECT_SOURCE_CELL, 0.f, 0.f, 0.f, 0, 0};
+    qp3d_run_options o{0, QP3D_DIRECT_SOURCE_CELL, 0.f, 0.f, 0.f, 0, 0, 0};
     if (opt) o = *opt;
     qp3d_parameters P;
     int rc = qp3d_parse_parameter_file(path, &P, err, errlen);
@@ -215,7 +260,7 @@ extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options 
         shot_source(P, in);
         if (o.verbose) printf("direct wave: vp %g eps %g delta %g\n", vd, ed, dd);
         if ((rc = model_shot(ctx, P, in, c, c2, P.snapflag_direct, P.snap_direct,
-                             rec_direct.data(), err, errlen)))
+                             o.write_rsf == 1, rec_direct.data(), err, errlen)))
             goto done;
         if (write_file(P.recdir_file, rec_direct.data(), nrec, "wb")) {
             rc = fail(err, errlen, QP3D_ERR_IO, "cannot write %s", P.recdir_file);
@@ -257,7 +302,7 @@ extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options 
                     goto done;
                 }
             } else if ((rc = model_shot(ctx, P, ins[0], c, c2, P.snapflag_full, P.snap_full,
-                                        recs[0].data(), err, errlen))) {
+                                        o.write_rsf == 1, recs[0].data(), err, errlen))) {
                 goto done;
             }
             for (size_t i = 0; i < cnt; ++i) {
@@ -289,7 +334,46 @@ extern "C" int qp3d_run_parameter_file(const char *path, const qp3d_run_options 
             }
         }
     }
+    // RSF headers of the record files; the appended files count every shot
+    // they hold
+    if (o.write_rsf == 1) {
+        const long long per = (long long)nrec * sizeof(float);
+        const std::pair<long long, float> y{P.hy, P.dy}, x{P.hx, P.dx}, t{P.nt, P.dt};
+        bool ok = true;
+        for (const char *f : {P.recfull_file, P.recmut_file}) {
+            FILE *fp = fopen(f, "rb");
+            long long size = -1;
+            if (fp && fseek(fp, 0, SEEK_END) == 0) size = ftell(fp);
+            if (fp) fclose(fp);
+            ok = ok && size > 0 && size % per == 0 &&
+                 !rsf(f, {y, x, t, {size / per, 1.0f}}, {"y", "x", "t", "shot"});
+        }
+        if (P.muteflag == 1) ok = ok && !rsf(P.recdir_file, {y, x, t}, {"y", "x", "t"});
+        ok = ok && !rsf(P.recxz_file, {x, t}, {"x", "t"}) &&
+             !rsf(P.recyz_file, {y, t}, {"y", "t"});
+        if (!ok) rc = fail(err, errlen, QP3D_ERR_IO, "cannot write the RSF headers");
+    }
 done:
     qp3d_ctx_destroy(ctx);
     return rc;
+}
+
+extern "C" int qp3d_write_rsf_header(const char *datafile, int naxes, const long long *n,
+                                     const float *d, const char *const *labels)
+{
+    if (!datafile || !*datafile || !n || naxes < 1 || naxes > 9) return QP3D_ERR_ARG;
+    for (int a = 0; a < naxes; ++a)
+        if (n[a] < 1) return QP3D_ERR_ARG;
+    std::string h(datafile);
+    if (h.size() >= 4 && h.compare(h.size() - 4, 4, ".dat") == 0) h.resize(h.size() - 4);
+    h += ".rsf";
+    FILE *fp = fopen(h.c_str(), "w");
+    if (!fp) return QP3D_ERR_IO;
+    fprintf(fp, "in=\"%s\"\ndata_format=\"native_float\"\nesize=4\n", datafile);
+    for (int a = 0; a < naxes; ++a) {
+        fprintf(fp, "n%d=%lld\n", a + 1, n[a]);
+        if (d) fprintf(fp, "d%d=%.9g\no%d=0\n", a + 1, (double)d[a], a + 1);
+        if (labels && labels[a]) fprintf(fp, "label%d=\"%s\"\n", a + 1, labels[a]);
+    }
+    return (ferror(fp) | fclose(fp)) ? QP3D_ERR_IO : QP3D_OK;
 }

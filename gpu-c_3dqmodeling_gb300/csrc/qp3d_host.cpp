@@ -184,18 +184,23 @@ extern "C" int qp3d_readmodel3d(const char *filename, float *a, int ny, int nx, 
 // ---------------------------------------------------------------------------
 namespace qp3d {
 
-// Snapshot files named as 3dPureqPModeling_single_shot.cu:342-345
-// (<prefix><k>.dat and <prefix>_xz/_yz/_xy<k>.dat, raw native floats,
-// read_write.c:29-52); user points to the prefix (std::string).
+// Snapshot file names of 3dPureqPModeling_single_shot.cu:342-345:
+// <prefix><k>.dat and <prefix>_xz/_yz/_xy<k>.dat.
+std::string snapshot_file_name(const std::string &prefix, int kind, int step)
+{
+    static const char *suffix[4] = {"", "_xz", "_yz", "_xy"};
+    return prefix + suffix[kind < 0 || kind > 3 ? 0 : kind] + std::to_string(step) + ".dat";
+}
+
+// Snapshot files as raw native floats (read_write.c:29-52); user points to
+// the prefix (std::string).
 int write_snapshot_files(void *user, int step, int kind, const float *data, int n0, int n1,
                          int n2)
 {
     const std::string *prefix = static_cast<const std::string *>(user);
-    static const char *suffix[4] = {"", "_xz", "_yz", "_xy"};
     if (kind < 0 || kind > 3) return -1;
-    char name[1024];
-    snprintf(name, sizeof(name), "%s%s%d.dat", prefix->c_str(), suffix[kind], step);
-    FILE *fp = fopen(name, "wb");
+    const std::string name = snapshot_file_name(*prefix, kind, step);
+    FILE *fp = fopen(name.c_str(), "wb");
     if (!fp) return -1;
     const size_t n = (size_t)n0 * n1 * n2;
     const size_t w = fwrite(data, sizeof(float), n, fp);

@@ -89,7 +89,7 @@ class RunOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("direct_model", ctypes.c_int),
                 ("direct_vp", ctypes.c_float), ("direct_eps", ctypes.c_float),
                 ("direct_del", ctypes.c_float), ("verbose", ctypes.c_int),
-                ("shots_per_call", ctypes.c_int)]
+                ("shots_per_call", ctypes.c_int), ("write_rsf", ctypes.c_int)]
 
 
 # every symbol include/qp3d.h and include/qp3d_driver.h declare
@@ -103,7 +103,7 @@ EXPORTS = [
     "qp3d_event_elapsed",
     "qp3d_host_alloc", "qp3d_host_free", "qp3d_gradmax_noalloc", "qp3d_fdcoff1", "qp3d_fdcoff2", "qp3d_pmlcoff",
     "qp3d_source", "qp3d_extend_model", "qp3d_absmax", "qp3d_readmodel3d",
-    "qp3d_parse_parameter_file", "qp3d_run_parameter_file",
+    "qp3d_parse_parameter_file", "qp3d_run_parameter_file", "qp3d_write_rsf_header",
 ]
 
 _lib = None
@@ -167,6 +167,9 @@ def load():
                                                      ctypes.c_char_p, ctypes.c_size_t]),
         "qp3d_run_parameter_file": (ctypes.c_int, [ctypes.c_char_p, P(RunOptions),
                                                    ctypes.c_char_p, ctypes.c_size_t]),
+        "qp3d_write_rsf_header": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int,
+                                                 P(ctypes.c_longlong), P(ctypes.c_float),
+                                                 P(ctypes.c_char_p)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -234,13 +237,33 @@ def parse_parameter_file(path):
 
 
 def run_parameter_file(path, device=0, direct_model=DIRECT_SOURCE_CELL, direct=(0.0, 0.0, 0.0),
-                       verbose=False, shots_per_call=0):
+                       verbose=False, shots_per_call=0, write_rsf=False):
     """qp3d_run_parameter_file -> (rc, message)."""
     o = RunOptions(device, direct_model, direct[0], direct[1], direct[2], int(verbose),
-                   int(shots_per_call))
+                   int(shots_per_call), int(write_rsf))
     err = ctypes.create_string_buffer(512)
     rc = load().qp3d_run_parameter_file(str(path).encode(), ctypes.byref(o), err, len(err))
     return rc, err.value.decode()
+
+
+def write_rsf_header(datafile, axes):
+    """qp3d_write_rsf_header; axes = [(n, d, label), ...] fastest first -> rc."""
+    k = len(axes)
+    n = (ctypes.c_longlong * k)(*[int(a[0]) for a in axes])
+    d = (ctypes.c_float * k)(*[float(a[1]) for a in axes])
+    lab = (ctypes.c_char_p * k)(*[str(a[2]).encode() for a in axes])
+    return int(load().qp3d_write_rsf_header(str(datafile).encode(), k, n, d, lab))
+
+
+def read_rsf_header(path):
+    """key -> value (str, quotes removed) of an RSF header file."""
+    out = {}
+    for line in open(path):
+        line = line.strip()
+        if "=" in line:
+            key, v = line.split("=", 1)
+            out[key] = v.strip('"')
+    return out
 
 
 def pml_state_size(nx, ny, nz, pml):

@@ -54,7 +54,18 @@ typedef struct {
                                       full-wave snapshots are requested);
                                       1: one qp3d_forward per shot, as the
                                       reference; N > 1: at most N per call */
+    int write_rsf;                 /* 1: an RSF header beside every file the job
+                                      writes (qp3d_write_rsf_header) */
 } qp3d_run_options;
+
+/* Madagascar RSF header for a raw native-float file, in the form of the
+ * reference's model/grey3_tmp.rsf: in="<datafile>", data_format, esize, then
+ * n, d, o (0) and label of each axis, fastest axis first.  The header is
+ * <datafile> with its ".dat" suffix replaced by ".rsf" (".rsf" appended when
+ * there is none); in= holds datafile as given.  Returns QP3D_OK,
+ * QP3D_ERR_ARG (no name, naxes outside 1..9, an axis n < 1) or QP3D_ERR_IO. */
+int qp3d_write_rsf_header(const char *datafile, int naxes, const long long *n, const float *d,
+                          const char *const *labels);
 
 /* Parse a parameter file.  Returns QP3D_OK, QP3D_ERR_IO (cannot open) or
  * QP3D_ERR_ARG (a value is missing or out of range); err receives a message. */
@@ -63,7 +74,10 @@ int qp3d_parse_parameter_file(const char *path, qp3d_parameters *out, char *err,
 /* Run the whole modeling job a parameter file describes, writing the same
  * files as the reference program: Record_fullwave and Record_mute appended
  * shot after shot (read_write.c:66-77), Record_direct, the first shot's xz/yz
- * record slices, and snapshots through modeling3d's naming.  The records do
+ * record slices, and snapshots through modeling3d's naming.  With write_rsf
+ * each gets an RSF header: records [shot][t][x][y] (n4 counts every shot the
+ * appended file holds), record slices [t][x] and [t][y], snapshot volumes
+ * [z][x][y] and slices [z][x], [z][y], [x][y].  The records do
  * not depend on shots_per_call.  Unlike the
  * reference it stops with an error when a model window leaves the model or a
  * file cannot be read or written.  opt may be NULL (defaults). */

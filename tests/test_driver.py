@@ -41,23 +41,58 @@ def test_parse_errors(tmp_path):
     assert rc == -1
 
 
+def test_rsf_header_writer(tmp_path):
+    # host-only: the header text of qp3d_write_rsf_header
+    f = str(tmp_path / "Record_fullwave.dat")
+    assert qp3d.write_rsf_header(f, [(18, 10.0, "y"), (20, 12.5, "x"), (300, 5e-4, "t"),
+                                     (4, 1.0, "shot")]) == 0
+    h = qp3d.read_rsf_header(str(tmp_path / "Record_fullwave.rsf"))
+    assert h["in"] == f and h["data_format"] == "native_float" and h["esize"] == "4"
+    assert [h["n%d" % a] for a in range(1, 5)] == ["18", "20", "300", "4"]
+    assert float(h["d2"]) == 12.5 and float(h["d3"]) == np.float32(5e-4) and h["o1"] == "0"
+    assert [h["label%d" % a] for a in range(1, 5)] == ["y", "x", "t", "shot"]
+    g = str(tmp_path / "snap_xz")           # no .dat suffix: .rsf appended
+    assert qp3d.write_rsf_header(g, [(7, 1.0, "x")]) == 0
+    assert qp3d.read_rsf_header(g + ".rsf")["n1"] == "7"
+    assert qp3d.write_rsf_header(f, [(0, 1.0, "y")]) == -1        # empty axis
+    assert qp3d.write_rsf_header(str(tmp_path / "no" / "x.dat"), [(1, 1.0, "y")]) == -6
+
+
+def _check_rsf(d, c, nshots, snapfull):
+    nt, hx, hy, Nz0 = c["nt"], c["hx"], c["hy"], c["Nz0"]
+    for name in ("Record_fullwave", "Record_mute"):
+        h = qp3d.read_rsf_header(os.path.join(d, name + ".rsf"))
+        assert [int(h["n%d" % a]) for a in range(1, 5)] == [hy, hx, nt, nshots]
+        assert h["in"].endswith(name + ".dat") and h["label3"] == "t"
+    h = qp3d.read_rsf_header(os.path.join(d, "Record_direct.rsf"))
+    assert [int(h["n%d" % a]) for a in range(1, 4)] == [hy, hx, nt]
+    h = qp3d.read_rsf_header(os.path.join(d, "recordxz.rsf"))
+    assert (int(h["n1"]), int(h["n2"])) == (hx, nt)
+    if snapfull:
+        h = qp3d.read_rsf_header(os.path.join(d, "snapshot_fullwave20.rsf"))
+        assert [int(h["n%d" % a]) for a in range(1, 4)] == [hy, hx, Nz0]
+        h = qp3d.read_rsf_header(os.path.join(d, "snapshot_fullwave_yz20.rsf"))
+        assert (int(h["n1"]), int(h["n2"]), h["label2"]) == (hy, Nz0, "z")
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("direct,snapfull,per_call,nxshot", [
-    ("values", 1, 0, 1),     # full-wave snapshots: one qp3d_forward per shot
-    ("source", 1, 0, 1),
-    ("values", 0, 0, 2),     # no snapshots: all four shots in one qp3d_batch call
-    ("values", 0, 3, 2),     # groups of three and one
-    ("values", 0, 1, 2),     # one shot per call, as the reference
+@pytest.mark.parametrize("direct,snapfull,per_call,nxshot,rsf", [
+    ("values", 1, 0, 1, 1),  # full-wave snapshots: one qp3d_forward per shot
+    ("source", 1, 0, 1, 0),
+    ("values", 0, 0, 2, 1),  # no snapshots: all four shots in one qp3d_batch call
+    ("values", 0, 3, 2, 0),  # groups of three and one
+    ("values", 0, 1, 2, 0),  # one shot per call, as the reference
 ])
-def test_modeling_job_matches_oracle(tmp_path, direct, snapfull, per_call, nxshot):
+def test_modeling_job_matches_oracle(tmp_path, direct, snapfull, per_call, nxshot, rsf):
     d = str(tmp_path)
     path, c, models = write_case(d, snapfull=snapfull, nxshot=nxshot)
     if direct == "values":
         rc, msg = qp3d.run_parameter_file(path, direct_model=qp3d.DIRECT_VALUES,
-                                          direct=(2100.0, 0.1, 0.05), shots_per_call=per_call)
+                                          direct=(2100.0, 0.1, 0.05), shots_per_call=per_call,
+                                          write_rsf=rsf)
         dvals = (2100.0, 0.1, 0.05)
     else:
-        rc, msg = qp3d.run_parameter_file(path, shots_per_call=per_call)
+        rc, msg = qp3d.run_parameter_file(path, shots_per_call=per_call, write_rsf=rsf)
         fny, fnx = c["sy0"] - (c["hy"] - 1) // 2, c["sx0"] - (c["hx"] - 1) // 2
         cell = (fny + (c["hy"] - 1) // 2, fnx + (c["hx"] - 1) // 2, 0)
         dvals = tuple(float(m[cell]) for m in models)
@@ -71,6 +106,10 @@ def test_modeling_job_matches_oracle(tmp_path, direct, snapfull, per_call, nxsho
     shots = [(c["sx0"] + ix * c["dxshot"], c["sy0"] + iy * c["dyshot"])
              for ix in range(c["nxshot"]) for iy in range(c["nyshot"])]
     assert full.shape[0] == len(shots) and mute.shape[0] == len(shots)   # appended shot by shot
+    if rsf:
+        _check_rsf(d, c, len(shots), snapfull)
+    else:
+        assert not os.path.exists(os.path.join(d, "Record_fullwave.rsf"))
     last = None
     for i, (sx, sy) in enumerate(shots):
         prob = oracle_shot(O, c, models, sx, sy)
