@@ -1559,142 +1559,285 @@ __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
 // bit, so these kernels take the cheaper arithmetic: fast division
 // (__fdividef, 2 ulp) in S and its derivatives, fused multiply-adds in the
 // transposed stencils.  Both passes are bound by the L1 load path and
-// instruction issue (31 and 63 gathered taps per cell); a shared-memory
-// z-marching form (register queue along z) was measured slower on GB300.
+// instruction issue (31 and 63 gathered taps per cell), so each thread takes
+// four consecutive y cells with 16-byte loads (a quarter of the load
+// instructions); a shared-memory z-marching form (register queue along z)
+// was measured slower on GB300.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) qp3d_adj_a_kernel(const AdjParams a)
+__device__ __forceinline__ float4 ldg4_or0(const float *f, long long j, bool ok)
 {
-    const int y = blockIdx.x * 32 + threadIdx.x, x = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+    return ok ? __ldg(reinterpret_cast<const float4 *>(f + j)) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// The 20 values y-8 .. y+11 of a field around a quad (zero off the row).
+__device__ __forceinline__ void row_window(const float *f, long long i, int y, int ldy, float w[20])
+{
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+        const int yb = y - 8 + 4 * b;
+        const float4 v = ldg4_or0(f, i - 8 + 4 * b, yb >= 0 && yb < ldy);
+        w[4 * b] = v.x; w[4 * b + 1] = v.y; w[4 * b + 2] = v.z; w[4 * b + 3] = v.w;
+    }
+}
+
+// Pass A, four consecutive y cells (a quad) per thread, block and warp
+// shapes as pass B.  The derivatives of u^k take the operation order of
+// cell_derivs; the streamed volumes move as 16-byte loads and stores.  Every
+// entry a quad writes that its cells leave unchanged is written as zero,
+// which it already is (padding, PML state at interior cells, u_prev and
+// gradient at PML cells).
+#define QP3D_ST4(ptr, v) *reinterpret_cast<float4 *>((ptr) + i) = make_float4(v[0], v[1], v[2], v[3])
+__global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
+{
+    const int q = threadIdx.x & 7, r = threadIdx.x >> 3;
+    const int y = blockIdx.x * 32 + 4 * q, x = blockIdx.y * 32 + r, z = blockIdx.z;
     if (y >= a.ny || x >= a.nx) return;
     const long long i = (long long)z * a.plane + (long long)x * a.ldy + y;
     const int nx = a.nx, ny = a.ny, nz = a.nz, pml = a.pml;
-    float l = a.Lu[i];
-    if (a.resid && z == a.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
-        l += a.resid[(long long)(x - pml) * a.hy + (y - pml)];
-    float nu = a.Lup[i], nup = 0.f, nw1 = 0.f, nw1o = 0.f, np_ = 0.f, npo = 0.f, nw21 = 0.f,
-          nw3 = 0.f, nw3o = 0.f;
-    float c[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const bool upd = x >= kRadius && x < nx - kRadius && y >= kRadius && y < ny - kRadius &&
-                     z >= kRadius && z < nz - kRadius;
-    if (!upd) {
-        nu += l;   // a never-updated cell keeps its value
-    } else {
-        float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
-        cell_derivs(a.u, i, a.ldy, a.plane, a.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
-        const float K = a.K[i], E2 = a.E2[i], R8 = a.R8[i], e2 = 1.0f + E2;
-        const float h2 = fmaf(Uy, Uy, Ux * Ux), m2 = fmaf(Uz, Uz, h2);
-        float S = 1.0f, dSe = 0.0f, dSd = 0.0f;
-        if (m2 > *a.T2) {
-            const float aa = __fdividef(h2, m2), bb = 1.0f - aa, D = fmaf(E2, aa, 1.0f);
-            const float iD = __fdividef(1.0f, D);
-            const float ab8 = 8.0f * aa * bb * iD * iD;
-            const float q = 0.125f * R8 * ab8;
-            const float r = sqrtf(fmaxf(1.0f - q, 0.0f));
-            S = 0.5f + 0.5f * r;
-            const float dSdq = r > 0.0f ? __fdividef(-0.25f, r) : 0.0f;
-            dSe = dSdq * ab8 * (1.0f - 0.5f * aa * R8 * iD);
-            dSd = -dSdq * ab8;
-        }
-        const float KS = K * S;
-        const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
-        const int fy = y < pml ? 2 : (y >= ny - pml ? 3 : -1);
-        const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
-        int f, li;
-        cell_face(fx, x < pml ? pml - x : x - nx + pml, fy, y < pml ? pml - y : y - ny + pml, fz,
-                  z < pml ? pml - z : z - nz + pml, f, li);
-        if (f < 0) {
-            nu += 2.0f * l;
-            nup = -l;
-            c[3] = KS * e2 * l;
-            c[4] = c[3];
-            c[5] = KS * l;
-            const float Lh = Uxx + Uyy, Lap = fmaf(e2, Lh, Uzz);
-            a.gK[i] += l * S * Lap;
-            a.gE[i] += l * K * (2.0f * S * Lh + dSe * Lap);
-            a.gD[i] += l * K * dSd * Lap;
-        } else {
-            const float4 lc = a.layers[(f >> 1) * pml + li];
-            const bool isz = f >= 4;
-            const float A = isz ? KS : e2 * KS, Bt = isz ? e2 * KS : KS;
-            const float sgn = (f & 1) ? -1.0f : 1.0f;
-            const float W1 = a.Lw1[i] + l, W21 = a.Lw21[i] + l, W3 = a.Lw3[i] + l;
-            const float P = fmaf(a.dt, W21, a.Lp[i]);
-            nw1 = fmaf(-lc.x, W1, a.Lw1o[i]);
-            nw1o = lc.y * W1;
-            np_ = fmaf(-lc.x, P, a.Lpo[i]);
-            npo = lc.y * P;
-            nw21 = lc.z * W21;
-            nw3 = fmaf(2.0f, W3, a.Lw3o[i]);
-            nw3o = -W3;
-            const float cn = A * W1, c1 = sgn * A * lc.w * P, ct = Bt * W3;
-            if (f < 2) { c[3] += cn; c[0] += c1; c[4] += ct * e2; c[5] += ct; }
-            else if (f < 4) { c[4] += cn; c[1] += c1; c[3] += ct * e2; c[5] += ct; }
-            else { c[5] += cn; c[2] += c1; c[3] += ct; c[4] += ct; }
-        }
+    const Coefs &k = a.k;
+    const float4 lu = ldg4_or0(a.Lu, i, true), lup = ldg4_or0(a.Lup, i, true);
+    float l[4] = {lu.x, lu.y, lu.z, lu.w}, nu[4] = {lup.x, lup.y, lup.z, lup.w};
+    if (a.resid && z == a.sz && x >= pml && x < nx - pml) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (y + j >= pml && y + j < ny - pml)
+                l[j] += a.resid[(long long)(x - pml) * a.hy + (y + j - pml)];
     }
-    a.Nu[i] = nu;
-    if (!upd) return;
-    const bool in_pml = x < pml || x >= nx - pml || y < pml || y >= ny - pml || z < pml ||
-                        z >= nz - pml;
-    if (in_pml) {
-        a.Nw1[i] = nw1; a.Nw1o[i] = nw1o; a.Np[i] = np_; a.Npo[i] = npo;
-        a.Nw21[i] = nw21; a.Nw3[i] = nw3; a.Nw3o[i] = nw3o;
-        a.C[0][i] = c[0]; a.C[1][i] = c[1]; a.C[2][i] = c[2];
-    } else {
-        a.Nup[i] = nup;
+    const bool row_upd = x >= kRadius && x < nx - kRadius && z >= kRadius && z < nz - kRadius;
+    const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
+    const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
+    const int lix = x < pml ? pml - x : x - nx + pml, liz = z < pml ? pml - z : z - nz + pml;
+    bool upd[4];
+    int f[4], li[4];
+    bool any_int = false, any_pml = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int yj = y + j;
+        upd[j] = row_upd && yj >= kRadius && yj < ny - kRadius;
+        const int fy = yj < pml ? 2 : (yj >= ny - pml ? 3 : -1);
+        cell_face(fx, lix, fy, yj < pml ? pml - yj : yj - ny + pml, fz, liz, f[j], li[j]);
+        any_int = any_int || (upd[j] && f[j] < 0);
+        any_pml = any_pml || (upd[j] && f[j] >= 0);
+        if (!upd[j]) nu[j] += l[j];   // a never-updated cell keeps its value
     }
-    a.C[3][i] = c[3]; a.C[4][i] = c[4]; a.C[5][i] = c[5];
+    float c3[4] = {0.f, 0.f, 0.f, 0.f}, c4[4] = {0.f, 0.f, 0.f, 0.f}, c5[4] = {0.f, 0.f, 0.f, 0.f};
+    if (any_int || any_pml) {
+        // derivatives of u^k (all taps in range for updated cells)
+        float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
+        {
+            float w[20];
+            row_window(a.u, i, y, a.ldy, w);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                u0[j] = w[8 + j];
+                float g = 0.0f, l2 = __fmul_rn(k.ky, u0[j]);
+#pragma unroll
+                for (int m = 0; m < kRadius; ++m) {
+                    const float pa = w[8 + j + m + 1], pb = w[8 + j - m - 1];
+                    const float d = __fsub_rn(pa, pb);
+                    g = (m == 0) ? __fmul_rn(k.cy[0], d) : fmaf(k.cy[m], d, g);
+                    l2 = fmaf(k.c2y[m], __fadd_rn(pa, pb), l2);
+                }
+                Uy[j] = g;
+                Uyy[j] = l2;
+                Ux[j] = Uz[j] = 0.0f;
+                Uxx[j] = __fmul_rn(k.kx, u0[j]);
+                Uzz[j] = __fmul_rn(k.kz, u0[j]);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m) {
+            const long long dx = (long long)(m + 1) * a.ldy, dz = (long long)(m + 1) * a.plane;
+            const float4 xp = ldg4_or0(a.u, i + dx, true), xm = ldg4_or0(a.u, i - dx, true);
+            const float4 zp = ldg4_or0(a.u, i + dz, true), zm = ldg4_or0(a.u, i - dz, true);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float ddx = __fsub_rn(f4(xp, j), f4(xm, j));
+                const float ddz = __fsub_rn(f4(zp, j), f4(zm, j));
+                Ux[j] = (m == 0) ? __fmul_rn(k.cx[0], ddx) : fmaf(k.cx[m], ddx, Ux[j]);
+                Uz[j] = (m == 0) ? __fmul_rn(k.cz[0], ddz) : fmaf(k.cz[m], ddz, Uz[j]);
+                Uxx[j] = fmaf(k.c2x[m], __fadd_rn(f4(xp, j), f4(xm, j)), Uxx[j]);
+                Uzz[j] = fmaf(k.c2z[m], __fadd_rn(f4(zp, j), f4(zm, j)), Uzz[j]);
+            }
+        }
+        // frozen scalar operator and its eps / delta derivatives
+        const float4 Kv = ldg4_or0(a.K, i, true), Ev = ldg4_or0(a.E2, i, true),
+                     Rv = ldg4_or0(a.R8, i, true);
+        const float T2 = *a.T2;
+        float KS[4], e2[4], S[4], dSe[4], dSd[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float E2 = f4(Ev, j), R8 = f4(Rv, j);
+            e2[j] = 1.0f + E2;
+            const float h2 = fmaf(Uy[j], Uy[j], Ux[j] * Ux[j]), m2 = fmaf(Uz[j], Uz[j], h2);
+            S[j] = 1.0f;
+            dSe[j] = dSd[j] = 0.0f;
+            if (m2 > T2) {
+                const float aa = __fdividef(h2, m2), bb = 1.0f - aa, D = fmaf(E2, aa, 1.0f);
+                const float iD = __fdividef(1.0f, D);
+                const float ab8 = 8.0f * aa * bb * iD * iD;
+                const float qq = 0.125f * R8 * ab8;
+                const float rr = sqrtf(fmaxf(1.0f - qq, 0.0f));
+                S[j] = 0.5f + 0.5f * rr;
+                const float dSdq = rr > 0.0f ? __fdividef(-0.25f, rr) : 0.0f;
+                dSe[j] = dSdq * ab8 * (1.0f - 0.5f * aa * R8 * iD);
+                dSd[j] = -dSdq * ab8;
+            }
+            KS[j] = f4(Kv, j) * S[j];
+        }
+        if (any_int) {   // interior leapfrog and the gradient sums
+            const float4 vK = ldg4_or0(a.gK, i, true), vE = ldg4_or0(a.gE, i, true),
+                         vD = ldg4_or0(a.gD, i, true);
+            float gK[4] = {vK.x, vK.y, vK.z, vK.w}, gE[4] = {vE.x, vE.y, vE.z, vE.w},
+                  gD[4] = {vD.x, vD.y, vD.z, vD.w}, nup[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (!(upd[j] && f[j] < 0)) continue;
+                nu[j] += 2.0f * l[j];
+                nup[j] = -l[j];
+                c3[j] = KS[j] * e2[j] * l[j];
+                c4[j] = c3[j];
+                c5[j] = KS[j] * l[j];
+                const float Lh = Uxx[j] + Uyy[j], Lap = fmaf(e2[j], Lh, Uzz[j]);
+                const float Kc = f4(Kv, j);
+                gK[j] += l[j] * S[j] * Lap;
+                gE[j] += l[j] * Kc * (2.0f * S[j] * Lh + dSe[j] * Lap);
+                gD[j] += l[j] * Kc * dSd[j] * Lap;
+            }
+            QP3D_ST4(a.gK, gK); QP3D_ST4(a.gE, gE); QP3D_ST4(a.gD, gD); QP3D_ST4(a.Nup, nup);
+        }
+        if (any_pml) {   // transposed split-field recursions
+            const float4 vw1 = ldg4_or0(a.Lw1, i, true), vw21 = ldg4_or0(a.Lw21, i, true),
+                         vw3 = ldg4_or0(a.Lw3, i, true), vp = ldg4_or0(a.Lp, i, true),
+                         vw1o = ldg4_or0(a.Lw1o, i, true), vpo = ldg4_or0(a.Lpo, i, true),
+                         vw3o = ldg4_or0(a.Lw3o, i, true);
+            float nw1[4], nw1o[4], np_[4], npo[4], nw21[4], nw3[4], nw3o[4], c0[4], c1[4], c2[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                nw1[j] = nw1o[j] = np_[j] = npo[j] = nw21[j] = nw3[j] = nw3o[j] = 0.0f;
+                c0[j] = c1[j] = c2[j] = 0.0f;
+                if (!(upd[j] && f[j] >= 0)) continue;
+                const float4 lc = a.layers[(f[j] >> 1) * pml + li[j]];
+                const bool isz = f[j] >= 4;
+                const float A = isz ? KS[j] : e2[j] * KS[j], Bt = isz ? e2[j] * KS[j] : KS[j];
+                const float sgn = (f[j] & 1) ? -1.0f : 1.0f;
+                const float W1 = f4(vw1, j) + l[j], W21 = f4(vw21, j) + l[j], W3 = f4(vw3, j) + l[j];
+                const float P = fmaf(a.dt, W21, f4(vp, j));
+                nw1[j] = fmaf(-lc.x, W1, f4(vw1o, j));
+                nw1o[j] = lc.y * W1;
+                np_[j] = fmaf(-lc.x, P, f4(vpo, j));
+                npo[j] = lc.y * P;
+                nw21[j] = lc.z * W21;
+                nw3[j] = fmaf(2.0f, W3, f4(vw3o, j));
+                nw3o[j] = -W3;
+                const float cn = A * W1, cf = sgn * A * lc.w * P, ct = Bt * W3;
+                if (f[j] < 2) { c3[j] = cn; c0[j] = cf; c4[j] = ct * e2[j]; c5[j] = ct; }
+                else if (f[j] < 4) { c4[j] = cn; c1[j] = cf; c3[j] = ct * e2[j]; c5[j] = ct; }
+                else { c5[j] = cn; c2[j] = cf; c3[j] = ct; c4[j] = ct; }
+            }
+            QP3D_ST4(a.Nw1, nw1); QP3D_ST4(a.Nw1o, nw1o); QP3D_ST4(a.Np, np_);
+            QP3D_ST4(a.Npo, npo); QP3D_ST4(a.Nw21, nw21); QP3D_ST4(a.Nw3, nw3);
+            QP3D_ST4(a.Nw3o, nw3o);
+            QP3D_ST4(a.C[0], c0); QP3D_ST4(a.C[1], c1); QP3D_ST4(a.C[2], c2);
+        }
+        QP3D_ST4(a.C[3], c3); QP3D_ST4(a.C[4], c4); QP3D_ST4(a.C[5], c5);
+    }
+    QP3D_ST4(a.Nu, nu);
+#undef QP3D_ST4
 }
 
-// Pass B: Nu += the transposed stencils of the six coefficient fields.
-// Outside the PML shell the first-derivative fields (Cx, Cy, Cz) are zero and
-// Cyy equals Cxx (qp3d_adj_a_kernel), so a block whose whole footprint (its
-// cells and 5 cells around them) lies inside reads two fields and no bounds.
+// Pass B: Nu += the transposed stencils of the six coefficient fields, four
+// consecutive y cells (a quad) per thread with 16-byte loads; a block is 8
+// quads (32 y) x 32 rows, a warp 8 quads x 4 rows.  Taps outside the volume
+// read zero (the coefficient fields are zero in the row padding).  Outside
+// the PML shell the first-derivative fields Cx, Cy, Cz are zero and Cyy
+// equals Cxx (qp3d_adj_a_kernel), so a warp whose whole footprint (its cells
+// and 5 around them) lies inside reads two fields.
 __global__ void __launch_bounds__(256) qp3d_adj_b_kernel(const AdjParams a)
 {
-    const int y0 = blockIdx.x * 32, x0 = blockIdx.y * 8, z = blockIdx.z;
-    const int y = y0 + threadIdx.x, x = x0 + threadIdx.y;
+    const int q = threadIdx.x & 7, r = threadIdx.x >> 3;
+    const int y = blockIdx.x * 32 + 4 * q, x = blockIdx.y * 32 + r, z = blockIdx.z;
     if (y >= a.ny || x >= a.nx) return;
+    const int xw = blockIdx.y * 32 + ((threadIdx.x >> 5) << 2), yw = blockIdx.x * 32;
     const long long i = (long long)z * a.plane + (long long)x * a.ldy + y;
     const Coefs &k = a.k;
-    if (x0 - kRadius >= a.pml && x0 + 8 + kRadius <= a.nx - a.pml && y0 - kRadius >= a.pml &&
-        y0 + 32 + kRadius <= a.ny - a.pml && z - kRadius >= a.pml &&
-        z + kRadius < a.nz - a.pml) {
+    const bool inside = xw - kRadius >= a.pml && xw + 4 + kRadius <= a.nx - a.pml &&
+                        yw - kRadius >= a.pml && yw + 32 + kRadius <= a.ny - a.pml &&
+                        z - kRadius >= a.pml && z + kRadius < a.nz - a.pml;
+    float acc[4];
+    if (inside) {
         const float *H = a.C[3], *V = a.C[5];
-        const float h0 = H[i];
-        float acc = k.kx * h0 + k.ky * h0 + k.kz * V[i];
+        float w[20];
+        row_window(H, i, y, a.ldy, w);
+        const float4 v0 = ldg4_or0(V, i, true);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[j] = k.kx * w[8 + j] + k.ky * w[8 + j] + k.kz * f4(v0, j);
 #pragma unroll
         for (int m = 0; m < kRadius; ++m) {
             const int d = m + 1;
             const long long dx = (long long)d * a.ldy, dz = (long long)d * a.plane;
-            acc = fmaf(k.c2x[m], H[i + dx] + H[i - dx], acc);
-            acc = fmaf(k.c2y[m], H[i + d] + H[i - d], acc);
-            acc = fmaf(k.c2z[m], V[i + dz] + V[i - dz], acc);
-        }
-        a.Nu[i] += acc;
-        return;
-    }
-    const float *Cx = a.C[0], *Cy = a.C[1], *Cz = a.C[2], *Cxx = a.C[3], *Cyy = a.C[4],
-                *Czz = a.C[5];
-    float acc = k.kx * Cxx[i] + k.ky * Cyy[i] + k.kz * Czz[i];
+            const float4 hp = ldg4_or0(H, i + dx, true), hm = ldg4_or0(H, i - dx, true);
+            const float4 vp = ldg4_or0(V, i + dz, true), vm = ldg4_or0(V, i - dz, true);
 #pragma unroll
-    for (int m = 0; m < kRadius; ++m) {
-        const int d = m + 1;
-        float sxx = 0.f, sx = 0.f, syy = 0.f, sy = 0.f, szz = 0.f, sz = 0.f;
-        if (x + d < a.nx) { const long long j = i + (long long)d * a.ldy; sxx += Cxx[j]; sx -= Cx[j]; }
-        if (x - d >= 0) { const long long j = i - (long long)d * a.ldy; sxx += Cxx[j]; sx += Cx[j]; }
-        if (y + d < a.ny) { syy += Cyy[i + d]; sy -= Cy[i + d]; }
-        if (y - d >= 0) { syy += Cyy[i - d]; sy += Cy[i - d]; }
-        if (z + d < a.nz) { const long long j = i + (long long)d * a.plane; szz += Czz[j]; sz -= Cz[j]; }
-        if (z - d >= 0) { const long long j = i - (long long)d * a.plane; szz += Czz[j]; sz += Cz[j]; }
-        acc = fmaf(k.c2x[m], sxx, acc);
-        acc = fmaf(k.c2y[m], syy, acc);
-        acc = fmaf(k.c2z[m], szz, acc);
-        acc = fmaf(k.cx[m], sx, acc);
-        acc = fmaf(k.cy[m], sy, acc);
-        acc = fmaf(k.cz[m], sz, acc);
+            for (int j = 0; j < 4; ++j) {
+                acc[j] = fmaf(k.c2x[m], f4(hp, j) + f4(hm, j), acc[j]);
+                acc[j] = fmaf(k.c2y[m], w[8 + j + d] + w[8 + j - d], acc[j]);
+                acc[j] = fmaf(k.c2z[m], f4(vp, j) + f4(vm, j), acc[j]);
+            }
+        }
+    } else {
+        const float *Cx = a.C[0], *Cy = a.C[1], *Cz = a.C[2], *Cxx = a.C[3], *Cyy = a.C[4],
+                    *Czz = a.C[5];
+        {
+            float wyy[20];
+            row_window(Cyy, i, y, a.ldy, wyy);
+            const float4 xx0 = ldg4_or0(Cxx, i, true), zz0 = ldg4_or0(Czz, i, true);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                acc[j] = k.kx * f4(xx0, j) + k.ky * wyy[8 + j] + k.kz * f4(zz0, j);
+#pragma unroll
+            for (int m = 0; m < kRadius; ++m)
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    acc[j] = fmaf(k.c2y[m], wyy[8 + j + m + 1] + wyy[8 + j - m - 1], acc[j]);
+        }
+        {
+            float wy[20];
+            row_window(Cy, i, y, a.ldy, wy);
+#pragma unroll
+            for (int m = 0; m < kRadius; ++m)
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    acc[j] = fmaf(k.cy[m], wy[8 + j - m - 1] - wy[8 + j + m + 1], acc[j]);
+        }
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m) {
+            const int d = m + 1;
+            const long long dx = (long long)d * a.ldy, dz = (long long)d * a.plane;
+            const bool xp = x + d < a.nx, xm = x - d >= 0, zp = z + d < a.nz, zm = z - d >= 0;
+            const float4 xxp = ldg4_or0(Cxx, i + dx, xp), xxm = ldg4_or0(Cxx, i - dx, xm);
+            const float4 x1p = ldg4_or0(Cx, i + dx, xp), x1m = ldg4_or0(Cx, i - dx, xm);
+            const float4 zzp = ldg4_or0(Czz, i + dz, zp), zzm = ldg4_or0(Czz, i - dz, zm);
+            const float4 z1p = ldg4_or0(Cz, i + dz, zp), z1m = ldg4_or0(Cz, i - dz, zm);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                acc[j] = fmaf(k.c2x[m], f4(xxp, j) + f4(xxm, j), acc[j]);
+                acc[j] = fmaf(k.c2z[m], f4(zzp, j) + f4(zzm, j), acc[j]);
+                acc[j] = fmaf(k.cx[m], f4(x1m, j) - f4(x1p, j), acc[j]);
+                acc[j] = fmaf(k.cz[m], f4(z1m, j) - f4(z1p, j), acc[j]);
+            }
+        }
     }
-    a.Nu[i] += acc;
+    float *nu = a.Nu + i;
+    if (y + 3 < a.ny) {
+        float4 v = *reinterpret_cast<float4 *>(nu);
+        v.x += acc[0]; v.y += acc[1]; v.z += acc[2]; v.w += acc[3];
+        *reinterpret_cast<float4 *>(nu) = v;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (y + j < a.ny) nu[j] += acc[j];
+    }
 }
 
 __global__ void qp3d_threshold_kernel(const float *gmax, float *T2, int n)
@@ -1921,11 +2064,12 @@ cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0, int 
 
 cudaError_t launch_adjoint_step(const AdjParams &a, cudaStream_t stream)
 {
-    const dim3 block(32, 8), grid((a.ny + 31) / 32, (a.nx + 7) / 8, a.nz);
-    qp3d_adj_a_kernel<<<grid, block, 0, stream>>>(a);
+    // one thread per quad of 4 y cells; a block is 8 quads x 32 rows
+    const dim3 grid((a.ny + 31) / 32, (a.nx + 31) / 32, a.nz);
+    qp3d_adj_a_kernel<<<grid, 256, 0, stream>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    qp3d_adj_b_kernel<<<grid, block, 0, stream>>>(a);
+    qp3d_adj_b_kernel<<<grid, 256, 0, stream>>>(a);
     return cudaGetLastError();
 }
 
