@@ -53,6 +53,8 @@ static void free_shot(qp3d_ctx *ctx)
     if (ctx->redo) cudaFree(ctx->redo);
     if (ctx->alt_count) cudaFree(ctx->alt_count);
     if (ctx->amask) cudaFree(ctx->amask);
+    if (ctx->apml) cudaFree(ctx->apml);
+    ctx->apml = nullptr;
     if (ctx->alist) cudaFree(ctx->alist);
     if (ctx->fix_count) cudaFree(ctx->fix_count);
     ctx->fix_count = nullptr;
@@ -264,6 +266,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         CK(cudaMalloc(&ctx->amask, (size_t)defer_mask_words(ctx->vol) * sizeof(unsigned)));
         CK(cudaMalloc(&ctx->am2, (size_t)ctx->vol * sizeof(float)));
         CK(cudaMalloc(&ctx->av, (size_t)ctx->vol * sizeof(float)));
+        CK(cudaMalloc(&ctx->apml, (size_t)ctx->vol * sizeof(float4)));
         CK(cudaMalloc(&ctx->fix_count, ntb * sizeof(unsigned)));
         CK(cudaMalloc(&ctx->sres, 2 * ntb * sizeof(float)));
         // compacted list: a quarter of the cells (more deferred cells than
@@ -433,6 +436,7 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
         p.amask = ctx->amask;
         p.am2 = ctx->am2;
         p.av = ctx->av;
+        p.apml = ctx->apml;
         p.alt_count = ctx->alt_count + k;
         p.alist = ctx->alist;
         p.alist_cap = ctx->alist_cap;

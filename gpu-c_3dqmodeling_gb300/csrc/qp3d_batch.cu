@@ -128,6 +128,7 @@ void carve(Plan &s, Carver &c, size_t *zero_bytes)
     d.spec_err = c.take<float>(1);
     d.am2 = c.take<float>(vol);
     d.av = c.take<float>(vol);
+    d.apml = c.take<float4>(vol);
     d.alist_cap = (unsigned)std::min<size_t>(std::max<size_t>(1u << 16, vol / 4), 0x7fffffff);
     d.alist = c.take<unsigned>(d.alist_cap);
     d.layers = c.take<float4>(3 * (size_t)std::max(s.g.pml, 1));

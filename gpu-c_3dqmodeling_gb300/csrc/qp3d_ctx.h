@@ -53,6 +53,7 @@ struct qp3d_ctx {
     float *spec_err = nullptr;
     unsigned *amask = nullptr;       // deferred-cell bits, vol / 32 words
     float *am2 = nullptr, *av = nullptr;
+    float4 *apml = nullptr;
     unsigned *fix_count = nullptr;   // per step: deferred cells below the threshold
     float *sres = nullptr;           // per step: T2 and the window hit
     unsigned *alist = nullptr;       // compacted deferred cells

@@ -102,11 +102,12 @@ struct PlaneParams {
     float spec_bias;          // relative shift of the window (test hook, 0)
     // Cells whose decision waits for the exact max of the step ("deferred"):
     // one bit per cell, 32 y-cells per word (word = pitched index / 32), and
-    // at the cell's own index its m2 and its alternative value -- interior
-    // cell: u(k+1) with S = 1 (source included); PML cells are recomputed by
-    // the fix-up.
+    // at the cell's own index its m2 and its alternative value: u(k+1) with
+    // S = 1 (source included); a PML cell also keeps the split-field outputs
+    // of S = 1 {w13, w21, w33, p3} in apml.
     unsigned *amask;
     float *am2, *av;
+    float4 *apml;
     unsigned *alt_count;      // &alt_count[step]: deferred cells (compaction)
     unsigned *fix_count;      // &fix_count[step]: of them below the threshold
     float *sres;              // &sres[2*step]: T2 of the true max, 1 if inside the window
@@ -139,6 +140,7 @@ struct BatchShot {
     float *spec_err;
     unsigned *amask;          // vol / 32 words
     float *am2, *av;          // vol each
+    float4 *apml;             // vol
     unsigned *fix_count;      // nt
     float *sres;              // 2 * nt
     unsigned *alist;          // alist_cap entries

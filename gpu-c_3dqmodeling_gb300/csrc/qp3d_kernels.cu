@@ -718,6 +718,43 @@ __device__ __forceinline__ float pml_cell(int f, float4 lc, float KS, float e2, 
     return __fadd_rn(__fadd_rn(nw13, nw21), nw33);
 }
 
+// The same update with two scalar operators, KS and KS1 (S = 1): the terms
+// that do not depend on S are shared, and each result equals pml_cell's with
+// that operator bit for bit.  The second set of outputs goes to a1x.
+__device__ __forceinline__ float pml_cell2(int f, float4 lc, float KS, float KS1, float e2,
+                                           float Ux, float Uy, float Uz, float Uxx, float Uyy,
+                                           float Uzz, float dt, float w11, float w12, float w21,
+                                           float w31, float w32, float p1, float p2,
+                                           float &nw13, float &nw21, float &nw33, float &np3,
+                                           float &v1, float4 &a1x)
+{
+    const bool isx = f < 2, isz = f >= 4;
+    const float Unn = isx ? Uxx : (isz ? Uzz : Uyy);
+    const float Un = isx ? Ux : (isz ? Uz : Uy);
+    const float Tt = isz ? __fadd_rn(Uxx, Uyy) : fmaf(e2, isx ? Uyy : Uxx, Uzz);
+    const float a1 = lc.x, a2 = lc.y, a3 = lc.z, dd = lc.w;
+    const float X1 = fmaf(-a1, w12, __fmul_rn(a2, w11));
+    const float X2 = fmaf(-a1, p2, __fmul_rn(a2, p1));
+    const float X3 = fmaf(2.0f, w32, -w31);
+    const float W = __fmul_rn(a3, w21);
+    float out[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const float ks = s ? KS1 : KS;
+        const float e2KS = __fmul_rn(e2, ks);
+        const float A = isz ? ks : e2KS, Bt = isz ? e2KS : ks;
+        float Ad = __fmul_rn(A, dd);
+        Ad = (f & 1) ? -Ad : Ad;
+        const float n13 = fmaf(A, Unn, X1), n3 = fmaf(Ad, Un, X2);
+        const float n21 = fmaf(dt, n3, W), n33 = fmaf(Bt, Tt, X3);
+        out[s] = __fadd_rn(__fadd_rn(n13, n21), n33);
+        if (s) a1x = make_float4(n13, n21, n33, n3);
+        else nw13 = n13, nw21 = n21, nw33 = n33, np3 = n3;
+    }
+    v1 = out[1];
+    return out[0];
+}
+
 __device__ __forceinline__ float4 ldg4(const float *p)
 {
     return __ldg(reinterpret_cast<const float4 *>(p));
@@ -858,19 +895,6 @@ __device__ __forceinline__ void quad_params_half(const PlaneParams &p, uint2 hv,
     K = make_float4(k[0], k[1], k[2], k[3]);
     E2 = make_float4(e[0], e[1], e[2], e[3]);
     R8 = make_float4(r[0], r[1], r[2], r[3]);
-}
-
-// (vp dt)^2 and 2 eps of one cell, from either storage
-__device__ __forceinline__ float cell_K(const PlaneParams &p, long long i)
-{
-    if (!p.half_params) return p.prm_k[i];
-    const float vdt = __fmul_rn(__half2float(p.h_vp[i]), p.dt);
-    return __fmul_rn(vdt, vdt);
-}
-
-__device__ __forceinline__ float cell_E2(const PlaneParams &p, long long i)
-{
-    return p.half_params ? __fmul_rn(2.0f, __half2float(p.h_eps[i])) : p.prm_e[i];
 }
 
 template <bool SPEC, bool REUSE, bool HALF = false>
@@ -1034,10 +1058,27 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                 cell_face(fx, lix, fy[j], liy[j], fz, liz, f, li);
                 const bool is_pml = pml_quad && cell_ok[j] && f >= 0;
                 const float4 lc = tab[is_pml ? (f >> 1) * pml + li : 0];
-                const float v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e2[j], Ux[j], Uy[j], Uz[j],
-                                         Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
-                                         f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
-                                         n13[j], n21[j], n33[j], n3[j]);
+                float v;
+                if (SPEC) {
+                    // also the S = 1 update of the cell and its split-field
+                    // outputs, kept for a deferred cell's fix-up (computing
+                    // both for every cell keeps the loop free of branches)
+                    float v1;
+                    float4 a1x;
+                    v = pml_cell2(f < 0 ? 0 : f, lc, KS[j], __fmul_rn(f4(Kv, j), 1.0f), e2[j],
+                                  Ux[j], Uy[j], Uz[j], Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j),
+                                  f4(w12, j), f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
+                                  f4(p2, j), n13[j], n21[j], n33[j], n3[j], v1, a1x);
+                    if (is_pml && amb[j]) {
+                        alt[j] = v1;
+                        p.apml[base + j] = a1x;
+                    }
+                } else {
+                    v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e2[j], Ux[j], Uy[j], Uz[j], Uxx[j],
+                                 Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j), f4(w21, j),
+                                 f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j), n13[j], n21[j],
+                                 n33[j], n3[j]);
+                }
                 out[j] = is_pml ? v : out[j];
                 n13[j] = is_pml ? n13[j] : 0.0f;
                 n33[j] = is_pml ? n33[j] : 0.0f;
@@ -1127,34 +1168,6 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (z0 >= z1) return;
     step_tile<SPEC, false, HALF>(&tm_u, p, p.k, p.tile_x, y0, x0, z0, z1,
                                  blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
-}
-
-// Derivatives of u at one cell from global memory, in the same operation
-// order as quad_derivs (and the oracle's mirror).
-__device__ void cell_derivs(const float *u, long long i, long long sx, long long sz,
-                            const Coefs &k, float &Ux, float &Uy, float &Uz, float &Uxx,
-                            float &Uyy, float &Uzz, float &u0)
-{
-    u0 = u[i];
-    float g[3], l[3];
-    const long long st[3] = {sx, 1, sz};
-    const float *cc[3] = {k.cx, k.cy, k.cz};
-    const float *c2[3] = {k.c2x, k.c2y, k.c2z};
-    const float kk[3] = {k.kx, k.ky, k.kz};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        g[a] = 0.0f;
-        l[a] = __fmul_rn(kk[a], u0);
-#pragma unroll
-        for (int m = 0; m < kRadius; ++m) {
-            const float pa = u[i + (m + 1) * st[a]], pb = u[i - (m + 1) * st[a]];
-            const float d = __fsub_rn(pa, pb);
-            g[a] = (m == 0) ? __fmul_rn(cc[a][0], d) : fmaf(cc[a][m], d, g[a]);
-            l[a] = fmaf(c2[a][m], __fadd_rn(pa, pb), l[a]);
-        }
-    }
-    Ux = g[0]; Uy = g[1]; Uz = g[2];
-    Uxx = l[0]; Uyy = l[1]; Uzz = l[2];
 }
 
 // Resolution of a speculative step, one thread: whether the true max fell in
@@ -1252,11 +1265,11 @@ __global__ void qp3d_compact_kernel(const PlaneParams p) { compact_body(p, block
 
 // Fix-up of a speculative step.  If the true max lies in the window and the
 // list did not overflow, every listed cell (deferred and below the true
-// threshold) gets its S = 1 value: interior cells the stored one, PML cells
-// recomputed from the step's untouched inputs; otherwise *redo = 1 (set here
-// or by the resolution) and the gated exact re-run recomputes the whole step.
-__device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k, int *redo,
-                                           float *spec_err, unsigned block, unsigned nblocks)
+// threshold) gets the S = 1 results the step kernel stored for it (u(k+1),
+// and at PML cells the split-field state); otherwise *redo = 1 (set here or
+// by the resolution) and the gated exact re-run recomputes the whole step.
+__device__ __forceinline__ void fixup_body(const PlaneParams &p, int *redo, unsigned block,
+                                           unsigned nblocks)
 {
     const unsigned n = *p.fix_count;
     if (p.sres[1] == 0.0f) return;   // window missed: the step re-runs
@@ -1264,7 +1277,6 @@ __device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k,
         if (block == 0 && threadIdx.x == 0) *redo = 1;
         return;
     }
-    (void)spec_err;
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml, hy = ny - 2 * pml;
     const unsigned plane = (unsigned)p.plane, ldy = (unsigned)p.ldy;
     for (unsigned i = block * blockDim.x + threadIdx.x; i < n; i += nblocks * blockDim.x) {
@@ -1272,33 +1284,15 @@ __device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k,
         const int z = (int)(idx / plane);
         const unsigned rem = idx - (unsigned)z * plane;
         const int x = (int)(rem / ldy), y = (int)(rem - (unsigned)x * ldy);
-        const int fx = x < pml ? 0 : (x >= nx - pml ? 1 : -1);
-        const int fy = y < pml ? 2 : (y >= ny - pml ? 3 : -1);
-        const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
-        int f, li;
-        cell_face(fx, x < pml ? pml - x : x - nx + pml, fy, y < pml ? pml - y : y - ny + pml, fz,
-                  z < pml ? pml - z : z - nz + pml, f, li);
-        float out;
-        if (f < 0) {   // interior cell: its S = 1 value was stored
-            out = p.av[idx];
-        } else {
-            float Ux, Uy, Uz, Uxx, Uyy, Uzz, u0;
-            cell_derivs(p.u_cur, idx, p.ldy, p.plane, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
-            const float KS = __fmul_rn(cell_K(p, idx), 1.0f);
-            const float e2 = __fadd_rn(1.0f, cell_E2(p, idx));
-            float n13, n21, n33, n3;
-            out = pml_cell(f, p.layers[(f >> 1) * pml + li], KS, e2, Ux, Uy, Uz, Uxx, Uyy, Uzz,
-                           p.dt, p.w1o[idx], p.w1c[idx], p.w21o[idx], p.w3o[idx], p.w3c[idx],
-                           p.po[idx], p.pc[idx], n13, n21, n33, n3);
-            p.w1n[idx] = n13;
-            p.pn[idx] = n3;
-            p.w21n[idx] = n21;
-            p.w3n[idx] = n33;
-            for (int e = 0; e < p.nsrc; ++e) {   // the step kernel's source add
-                const SrcEntry s = p.src[e];
-                if (s.x == x && s.y == y && s.z == z)
-                    out = __fadd_rn(out, __fmul_rn(s.v, p.wavelet));
-            }
+        const bool in_pml = x < pml || x >= nx - pml || y < pml || y >= ny - pml || z < pml ||
+                            z >= nz - pml;
+        const float out = p.av[idx];   // the step kernel's S = 1 value, source included
+        if (in_pml) {                  // and a PML cell's split-field outputs
+            const float4 s = p.apml[idx];
+            p.w1n[idx] = s.x;
+            p.w21n[idx] = s.y;
+            p.w3n[idx] = s.z;
+            p.pn[idx] = s.w;
         }
         p.u_out[idx] = out;
         if (p.record && z == p.sz && x >= pml && x < nx - pml && y >= pml && y < ny - pml)
@@ -1306,9 +1300,9 @@ __device__ __forceinline__ void fixup_body(const PlaneParams &p, const Coefs &k,
     }
 }
 
-__global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo, float *spec_err)
+__global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo)
 {
-    fixup_body(p, p.k, redo, spec_err, blockIdx.x, gridDim.x);
+    fixup_body(p, redo, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1439,6 +1433,7 @@ __global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, Pl
             p.amask = b.amask;
             p.am2 = b.am2;
             p.av = b.av;
+            p.apml = b.apml;
             p.alt_count = b.alt_count + k;
             p.alist = b.alist;
             p.alist_cap = b.alist_cap;
@@ -1537,8 +1532,7 @@ __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
 {
     const PlaneParams &p = b.pp[blockIdx.y];
     if (!p.active || !p.spec) return;
-    fixup_body(p, b.k, const_cast<int *>(p.gate), const_cast<float *>(p.spec_err), blockIdx.x,
-               gridDim.x);
+    fixup_body(p, const_cast<int *>(p.gate), blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1582,7 +1576,7 @@ __device__ __forceinline__ void row_window(const float *f, long long i, int y, i
 
 // Pass A, four consecutive y cells (a quad) per thread, block and warp
 // shapes as pass B.  The derivatives of u^k take the operation order of
-// cell_derivs; the streamed volumes move as 16-byte loads and stores.  Every
+// quad_derivs; the streamed volumes move as 16-byte loads and stores.  Every
 // entry a quad writes that its cells leave unchanged is written as zero,
 // which it already is (padding, PML state at interior cells, u_prev and
 // gradient at PML cells).
@@ -1975,7 +1969,7 @@ cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaS
     if (e != cudaSuccess) return e;
     qp3d_compact_kernel<<<(unsigned)((words / 4 + 255) / 256), 256, 0, stream>>>(p);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    qp3d_fixup_kernel<<<8 * nsm, 256, 0, stream>>>(p, redo, spec_err);
+    qp3d_fixup_kernel<<<8 * nsm, 256, 0, stream>>>(p, redo);
     return cudaGetLastError();
 }
 
