@@ -260,7 +260,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         CK(cudaMalloc(&ctx->win, 3 * ntb * sizeof(float)));
         CK(cudaMalloc(&ctx->redo, ntb * sizeof(int)));
         CK(cudaMalloc(&ctx->alt_count, ntb * sizeof(unsigned)));
-        CK(cudaMalloc(&ctx->spec_err, sizeof(float)));
+        CK(cudaMalloc(&ctx->spec_err, kSpecHist * sizeof(float)));
         // deferred cells of a speculative step: one bit per cell (vol is a
         // multiple of 32), m2 and the alternative value at the cell's index
         CK(cudaMalloc(&ctx->amask, (size_t)defer_mask_words(ctx->vol) * sizeof(unsigned)));
@@ -365,8 +365,9 @@ extern "C" int qp3d_shot_reset(qp3d_ctx *ctx)
     CK(cudaMemsetAsync(ctx->fix_count, 0, ntb * sizeof(unsigned), ctx->stream));
     CK(cudaMemsetAsync(ctx->amask, 0, (size_t)defer_mask_words(ctx->vol) * sizeof(unsigned),
                        ctx->stream));
-    static const float one = 1.0f;
-    CK(cudaMemcpyAsync(ctx->spec_err, &one, sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    // error history: no prediction yet (1.0 opens the widest window once)
+    static const float first[kSpecHist] = {1.0f};
+    CK(cudaMemcpyAsync(ctx->spec_err, first, sizeof(first), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(ctx->gmax, 0, sizeof(float) * std::max(ctx->g.nt, 1), ctx->stream));
     CK(cudaMemsetAsync(ctx->record, 0,
                        sizeof(float) * (size_t)std::max(ctx->g.nt, 1) * ctx->hx * ctx->hy,

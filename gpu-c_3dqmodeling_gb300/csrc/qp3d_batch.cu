@@ -125,7 +125,7 @@ void carve(Plan &s, Carver &c, size_t *zero_bytes)
     d.K = c.take<float>(vol);
     d.E2 = c.take<float>(vol);
     d.R8 = c.take<float>(vol);
-    d.spec_err = c.take<float>(1);
+    d.spec_err = c.take<float>(kSpecHist);
     d.am2 = c.take<float>(vol);
     d.av = c.take<float>(vol);
     d.apml = c.take<float4>(vol);
@@ -344,8 +344,9 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
         CKL(launch_params(nullptr, nullptr, nullptr, const_cast<float *>(d.K),
                           const_cast<float *>(d.E2), const_cast<float *>(d.R8), P.vol, P.g.dt,
                           ctx->stream));
-        static const float one = 1.0f;
-        CK(cudaMemcpyAsync(d.spec_err, &one, sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        static const float first[kSpecHist] = {1.0f};   // no prediction yet
+        CK(cudaMemcpyAsync(d.spec_err, first, sizeof(first), cudaMemcpyHostToDevice,
+                           ctx->stream));
         if (P.g.pml > 0) {
             std::vector<float4> tab(3 * P.g.pml);
             derive_layers(m.dlr, m.ddlr, P.g.pml, P.g.dt, tab.data());

@@ -37,6 +37,9 @@ constexpr int kRing = 2 * kRadius + 1 + kPrefetch;   // staged planes
 constexpr int kMaxTileX = 32;
 constexpr int kThreads = kQuadsY * kMaxTileX;        // 256
 constexpr int kMaxFusedSources = 64;
+// Relative prediction errors of the step max kept for the speculative window
+// (most recent first).
+constexpr int kSpecHist = 8;
 constexpr int kMaxPml = 256;
 
 // Error bits written to the device error word.
@@ -97,7 +100,7 @@ struct PlaneParams {
     int spec;                 // 1: predicted window, own max, deferred cells
     const int *gate;          // exact mode: run only if *gate != 0 (null: always)
     float *win;               // spec: &win[3*step] = (M_lo, M_hi, M_pred)
-    const float *spec_err;    // last relative prediction error of the max
+    const float *spec_err;    // kSpecHist last relative prediction errors of the max
     float delta_min;          // smallest half-width of the window
     float spec_bias;          // relative shift of the window (test hook, 0)
     // Cells whose decision waits for the exact max of the step ("deferred"):

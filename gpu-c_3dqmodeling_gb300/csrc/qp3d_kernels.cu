@@ -798,9 +798,15 @@ __device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &p
     const float m0 = k >= 2 ? p.gmax[k - 2] : 0.0f;
     float r = (m0 > 0.0f) ? __fdiv_rn(m1, m0) : 1.0f;
     r = fminf(fmaxf(r, 0.5f), 2.0f);
-    pred = __fmul_rn(m1, r);
-    // cover both "the max keeps its trend" and "the max stays where it was"
-    const float d = fminf(0.25f, fmaxf(p.delta_min, __fmul_rn(3.0f, *p.spec_err)));
+    // half the last trend: late in a shot the max moves by a few tenths of a
+    // percent per step with changing sign, which a full extrapolation doubles
+    pred = __fmul_rn(m1, fmaf(0.5f, __fsub_rn(r, 1.0f), 1.0f));
+    // cover both "the max keeps its trend" and "the max stays where it was",
+    // widened by 1.5x the largest of the recent prediction errors
+    float e = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kSpecHist; ++i) e = fmaxf(e, p.spec_err[i]);
+    const float d = fminf(0.25f, fmaxf(p.delta_min, __fmul_rn(1.5f, e)));
     lo = __fmul_rn(fminf(pred, m1), __fsub_rn(1.0f, d));
     hi = __fmul_rn(fmaxf(pred, m1), __fadd_rn(1.0f, d));
     if (p.spec_bias != 0.0f) {   // test hook: a window that misses on purpose
@@ -1181,7 +1187,9 @@ __device__ __forceinline__ void resolve_body(const PlaneParams &p, int *redo, fl
     p.sres[0] = threshold_m2(M);
     p.sres[1] = inside ? 1.0f : 0.0f;
     *redo = inside ? 0 : 1;   // the fix-up sets it too when the list overflows
-    *spec_err = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
+#pragma unroll
+    for (int i = kSpecHist - 1; i > 0; --i) spec_err[i] = spec_err[i - 1];
+    spec_err[0] = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
 }
 
 __global__ void qp3d_resolve_kernel(const PlaneParams p, int *redo, float *spec_err)
