@@ -37,9 +37,9 @@
 // dx*dx, CPU_function.c:314-316,393-395) are folded into the coefficient
 // tables, and a*b+c is fused where written as fmaf().  This translation unit
 // is compiled with -fmad=false so that no other fusion happens: the result is
-// bit-identical to the mirror variant of the CPU oracle.  The two divisions of
-// the scalar operator are Newton-Raphson reciprocals (rcp_nr: fused
-// multiply-adds only, so the oracle reproduces them exactly); the square root
+// bit-identical to the mirror variant of the CPU oracle.  The division of the
+// scalar operator is a Newton-Raphson reciprocal (rcp_nr2: fused
+// multiply-adds only, so the oracle reproduces it exactly); the square root
 // is IEEE (sqrt.rn).
 #include "qp3d_internal.h"
 
@@ -821,21 +821,10 @@ __device__ void spec_window(const PlaneParams &p, float &lo, float &hi, float &p
 // fast inverse square root).  Three steps take the guess's ~12% error below
 // float rounding.  About a third of the instructions of an IEEE division,
 // which dominated the scalar operator once most cells are above the
-// threshold; the mirror oracle performs the same operations.
-__device__ __forceinline__ float rcp_nr(float x)
-{
-    float r = __uint_as_float(0x7EF311C3u - __float_as_uint(x));
-#pragma unroll
-    for (int it = 0; it < 3; ++it) {
-        const float e = fmaf(-x, r, 1.0f);
-        r = fmaf(r, e, r);
-    }
-    return r;
-}
-
-// The same two operations on a pair of cells with the packed FP32x2
-// instructions (round-to-nearest per lane: each lane is bit-identical to the
-// scalar form).
+// threshold; the mirror oracle performs the same operations:
+//   r = bits(0x7EF311C3 - bits(x)); 3 x { e = fma(-x, r, 1); r = fma(r, e, r) }
+// Two cells at a time with the packed FP32x2 instructions (round-to-nearest
+// per lane: each lane performs the scalar operations above).
 __device__ __forceinline__ float2 rcp_nr2(float2 x)
 {
     float2 r = make_float2(__uint_as_float(0x7EF311C3u - __float_as_uint(x.x)),
@@ -849,29 +838,18 @@ __device__ __forceinline__ float2 rcp_nr2(float2 x)
     return r;
 }
 
-__device__ __forceinline__ float2 aniso_s2(float2 h2, float2 m2, float2 e2x, float2 r8)
+// S of two cells (GPU_kernel.cu:100-111), given they are above the threshold.
+// With a = (nx^2 + ny^2) = h2/m2, nz^2 = 1 - a = v2/m2 (v2 = Uz^2),
+// S = 1/2 + 1/2 sqrt(1 - 8(eps-delta) a (1-a) / (1 + 2 eps a)^2)
+//   = 1/2 + 1/2 sqrt(1 - 8(eps-delta) (h2 r) (v2 r)),  r = 1 / (m2 + 2 eps h2):
+// one reciprocal per cell, and both factors h2 r, v2 r lie in [0, 1].
+__device__ __forceinline__ float2 aniso_s2(float2 h2, float2 m2, float2 v2, float2 e2x, float2 r8)
 {
     const float2 one = make_float2(1.0f, 1.0f), half = make_float2(0.5f, 0.5f);
-    const float2 aa = __fmul2_rn(h2, rcp_nr2(m2));
-    const float2 bb = __fadd2_rn(one, make_float2(-aa.x, -aa.y));
-    const float2 den = __ffma2_rn(e2x, aa, one);
-    const float2 num = __fmul2_rn(__fmul2_rn(r8, aa), bb);
-    const float2 qq = __fmul2_rn(num, rcp_nr2(__fmul2_rn(den, den)));
+    const float2 r = rcp_nr2(__ffma2_rn(e2x, h2, m2));
+    const float2 qq = __fmul2_rn(__fmul2_rn(r8, __fmul2_rn(h2, r)), __fmul2_rn(v2, r));
     const float2 t = __fadd2_rn(one, make_float2(-qq.x, -qq.y));
     return __ffma2_rn(half, make_float2(__fsqrt_rn(t.x), __fsqrt_rn(t.y)), half);
-}
-
-// S of one cell (GPU_kernel.cu:100-111), given it is above the threshold:
-// with a = (nx^2 + ny^2) = h2/m2 and nz^2 = 1 - a,
-// S = 1/2 + 1/2 sqrt(1 - 8(eps-delta) a (1-a) / (1 + 2 eps a)^2).
-__device__ __forceinline__ float aniso_s(float h2, float m2, float e2x, float r8)
-{
-    float aa = __fmul_rn(h2, rcp_nr(m2));
-    float bb = __fsub_rn(1.0f, aa);
-    float den = fmaf(e2x, aa, 1.0f);
-    float num = __fmul_rn(__fmul_rn(r8, aa), bb);
-    float qq = __fmul_rn(num, rcp_nr(__fmul_rn(den, den)));
-    return fmaf(0.5f, __fsqrt_rn(__fsub_rn(1.0f, qq)), 0.5f);
 }
 
 // One tile column [z0, z1) of the step.  The grid kernel below runs one per
@@ -1037,6 +1015,8 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
             for (int h = 0; h < 2; ++h) {   // cells (0,1) and (2,3) as pairs
                 const int j0 = 2 * h, j1 = 2 * h + 1;
                 const float2 s = aniso_s2(make_float2(h2[j0], h2[j1]), make_float2(m2[j0], m2[j1]),
+                                          __fmul2_rn(make_float2(Uz[j0], Uz[j1]),
+                                                     make_float2(Uz[j0], Uz[j1])),
                                           make_float2(f4(Ev, j0), f4(Ev, j1)),
                                           make_float2(f4(Rv, j0), f4(Rv, j1)));
                 KS[j0] = __fmul_rn(f4(Kv, j0), above[j0] ? s.x : 1.0f);

@@ -541,11 +541,10 @@ static void mirror_update(st32 *s, const oracle_args *a, const mirror_coef *k,
                 float m2 = fmaf(Uz, Uz, h2);
                 float S = 1.0f;
                 if (m2 > T2) {
-                    float aa = h2 * mirror_rcp(m2);
-                    float bb = 1.0f - aa;
-                    float den = fmaf(e2x, aa, 1.0f);
-                    float num = (r8 * aa) * bb;
-                    float q = num * mirror_rcp(den * den);
+                    /* a(1-a)/(1+2eps a)^2 = (h2 r)(v2 r), r = 1/(m2 + 2eps h2) */
+                    float v2 = Uz * Uz;
+                    float r = mirror_rcp(fmaf(e2x, h2, m2));
+                    float q = (r8 * (h2 * r)) * (v2 * r);
                     S = fmaf(0.5f, sqrtf(1.0f - q), 0.5f);
                 }
                 float KS = K * S;
