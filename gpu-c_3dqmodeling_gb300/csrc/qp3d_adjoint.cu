@@ -126,6 +126,10 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
         return ctx_fail(ctx, QP3D_ERR_ARG,
                         "qp3d_adjoint: sources and receivers must lie inside the updated box");
     const int nt = g->nt;
+    if (nt == 0) {   // no record: zero misfit, nothing added to the gradient
+        if (misfit) *misfit = 0.0;
+        return QP3D_OK;
+    }
     const long long vol = ctx->vol;
     const size_t rec = (size_t)nt * ctx->hx * ctx->hy;
     const size_t vb = (size_t)vol * sizeof(float);

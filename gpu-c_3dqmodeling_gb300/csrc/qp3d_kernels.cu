@@ -2064,6 +2064,7 @@ cudaError_t launch_threshold(const float *gmax, float *T2, int n, cudaStream_t s
 cudaError_t launch_residual(const float *rec, const float *dobs, float *r, long long n,
                             double *misfit, cudaStream_t stream)
 {
+    if (n <= 0) return cudaSuccess;
     long long b = (n + 255) / 256;
     qp3d_residual_kernel<<<(int)(b > 4096 ? 4096 : b), 256, 0, stream>>>(rec, dobs, r, n, misfit);
     return cudaGetLastError();
@@ -2071,6 +2072,7 @@ cudaError_t launch_residual(const float *rec, const float *dobs, float *r, long 
 
 cudaError_t launch_to_bf16(const float *a, __nv_bfloat16 *h, long long n, cudaStream_t stream)
 {
+    if (n <= 0) return cudaSuccess;
     long long b = (n + 255) / 256;
     qp3d_to_bf16_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(a, h, n);
     return cudaGetLastError();
@@ -2078,6 +2080,7 @@ cudaError_t launch_to_bf16(const float *a, __nv_bfloat16 *h, long long n, cudaSt
 
 cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cudaStream_t stream)
 {
+    if (n <= 0) return cudaSuccess;
     long long b = (n + 255) / 256;
     qp3d_from_bf16_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(h, a, n);
     return cudaGetLastError();
@@ -2085,6 +2088,7 @@ cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cuda
 
 cudaError_t launch_to_half(const float *a, __half *h, long long n, cudaStream_t stream)
 {
+    if (n <= 0) return cudaSuccess;
     long long b = (n + 255) / 256;
     qp3d_to_half_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(a, h, n);
     return cudaGetLastError();

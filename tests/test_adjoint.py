@@ -83,6 +83,14 @@ def test_adjoint_schedules_agree(reference):
             assert np.array_equal(a, b)
 
 
+def test_adjoint_without_steps():
+    shot = synthetic.small_case(hx=16, hy=14, nz0=12, pml=6, nt=0, seed=52)
+    with qp3d.Context(0) as ctx:
+        J, g = ctx.adjoint(shot, np.zeros((0, shot.hx, shot.hy), np.float32))
+    assert J == 0.0
+    assert all(not np.any(gi) for gi in g)
+
+
 def test_adjoint_against_live_finite_differences(reference):
     shot, d_obs, _, _, inside = reference
     with qp3d.Context(0) as ctx:

@@ -64,8 +64,10 @@ def test_zero_steps(ctx):
 
 
 def test_edge_cases_through_batch(ctx):
-    names = ["one_step", "no_pml", "pml_5", "thin_x", "tall_z", "corner_source", "ragged_y"]
-    shots = [synthetic.small_case(**CASES[n]) for n in names]
+    names = ["one_step", "no_pml", "pml_5", "thin_x", "tall_z", "corner_source", "ragged_y",
+             "no_steps"]
+    shots = [synthetic.small_case(**CASES[n]) for n in names[:-1]]
+    shots.append(synthetic.small_case(hx=22, hy=26, nz0=18, pml=8, nt=0, seed=31))
     single = [ctx.forward(s) for s in shots]
     recs = ctx.batch(shots)
     for n, a, b in zip(names, recs, single):
