@@ -132,3 +132,61 @@ def test_context_without_device_fails_cleanly():
         pytest.skip("a GPU is present")
     with pytest.raises(qp3d.QP3DError):
         qp3d.Context(0)
+
+
+def test_reference_program_links_against_the_library(tmp_path):
+    """Link-time drop-in: the reference's own main program, compiled from its
+    unmodified sources in the reference checkout (outputs in tmp_path), links
+    against libqp3d.so with modeling3d resolved from the library; and a C
+    program using only include/qp3d.h compiles as C99 and links."""
+    from oracle import build as ob
+    if not ob.reference_available():
+        pytest.skip("reference checkout not present")
+    lib_dir = os.path.dirname(qp3d.LIB_PATH)
+    objs = []
+    for src in ("array_new.c", "read_write.c", "CPU_function.c", "3dPureqPModeling1.0.c"):
+        o = str(tmp_path / (src[:-2] + ".o"))
+        # the reference compiles its .c files as C++ (Makefile:9)
+        r = subprocess.run(["g++", "-w", "-c", "-I", ob.REFERENCE_DIR,
+                            os.path.join(ob.REFERENCE_DIR, src), "-o", o],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        objs.append(o)
+    exe = str(tmp_path / "3dqpmodeling")
+    r = subprocess.run(["g++", "-o", exe] + objs + ["-L" + lib_dir, "-lqp3d",
+                                                    "-Wl,-rpath," + lib_dir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    undefined = subprocess.run(["nm", "-C", "--undefined-only", exe], capture_output=True,
+                               text=True).stdout
+    assert "modeling3d(int, int, int" in undefined        # provided by libqp3d.so
+    defined = subprocess.run(["nm", "-C", "-D", "--defined-only", qp3d.LIB_PATH],
+                             capture_output=True, text=True).stdout
+    assert "modeling3d(int, int, int" in defined
+
+
+def test_c_program_against_the_public_header(tmp_path):
+    src = tmp_path / "use_abi.c"
+    src.write_text('''
+#include <stdio.h>
+#include "qp3d.h"
+#include "qp3d_driver.h"
+int main(void)
+{
+    qp3d_ctx *ctx = NULL;
+    int rc = qp3d_ctx_create(0, &ctx);
+    printf("%d %s\\n", rc, qp3d_strerror(rc));
+    if (rc == QP3D_OK) qp3d_ctx_destroy(ctx);
+    return 0;
+}
+''')
+    lib_dir = os.path.dirname(qp3d.LIB_PATH)
+    exe = str(tmp_path / "use_abi")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", exe, "-L" + lib_dir, "-lqp3d", "-Wl,-rpath," + lib_dir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0
+    rc = int(out.stdout.split()[0])
+    assert rc in (0, -2)   # QP3D_OK on a GPU machine, QP3D_ERR_CUDA without one
