@@ -80,8 +80,8 @@ struct qp3d_ctx {
     int threshold_mode = 1;          // 0: gradmax pre-pass every step, 1: speculative
     // smallest half-width of the predicted window: 1% for single shots, 2% for
     // batched ones (their small grids make the max jumpier: measured on 64
-    // config-3 shots 3417 exact re-runs at 1%, 1013 at 2%, 1.7% faster) unless
-    // set with "spec_delta_ppm"
+    // uneven shots of ~11 M cells, 2000 steps: 3417 exact re-runs at 1%, 1013
+    // at 2%, 1.7% faster) unless set with "spec_delta_ppm"
     float delta_min = 0.01f;
     bool delta_min_set = false;
     float spec_bias = 0.0f;          // test hook: shifts the predicted window
