@@ -274,22 +274,23 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         ctx->alist_cap = (unsigned)std::min<long long>(std::max(1ll << 16, ctx->vol / 4), 0x7fffffff);
         CK(cudaMalloc(&ctx->alist, (size_t)ctx->alist_cap * sizeof(unsigned)));
     }
-    if (half) {
-        // vp, eps, delta rounded to IEEE half (the wavefield buffers serve as
-        // FP32 staging; the reset below zeroes them)
+    // vp, eps, delta go to the device in one piece each (the wavefield buffers
+    // serve as staging; the reset below zeroes them) and are laid out pitched
+    // on the device: as IEEE half, or as the per-cell parameters
+    {
         const float *src[3] = {m->vp, m->epsilon, m->delta};
-        __half *dst[3] = {ctx->h_vp, ctx->h_eps, ctx->h_del};
-        for (int i = 0; i < 3; ++i) {
-            if ((rc = upload_vol(ctx, ctx->U[i], src[i]))) return rc;
-            CKL(launch_to_half(ctx->U[i], dst[i], ctx->vol, ctx->stream));
+        const size_t dense = (size_t)g->nx * g->ny * g->nz * sizeof(float);
+        for (int i = 0; i < 3; ++i)
+            CK(cudaMemcpyAsync(ctx->U[i], src[i], dense, cudaMemcpyHostToDevice, ctx->stream));
+        if (half) {
+            __half *dst[3] = {ctx->h_vp, ctx->h_eps, ctx->h_del};
+            for (int i = 0; i < 3; ++i)
+                CKL(launch_to_half_dense(ctx->U[i], dst[i], g->nx, g->ny, g->nz, ctx->ldy,
+                                         ctx->stream));
+        } else {
+            CKL(launch_params_dense(ctx->U[0], ctx->U[1], ctx->U[2], ctx->K, ctx->E2, ctx->R8,
+                                    g->nx, g->ny, g->nz, ctx->ldy, g->dt, ctx->stream));
         }
-    } else {
-        // model -> per-cell parameters (K, E2, R8 hold vp, eps, delta first)
-        if ((rc = upload_vol(ctx, ctx->K, m->vp)) || (rc = upload_vol(ctx, ctx->E2, m->epsilon)) ||
-            (rc = upload_vol(ctx, ctx->R8, m->delta)))
-            return rc;
-        CKL(launch_params(nullptr, nullptr, nullptr, ctx->K, ctx->E2, ctx->R8, ctx->vol, g->dt,
-                          ctx->stream));
     }
     // coefficient tables
     derive_coefs(m->c, m->c2, g->dx, g->dy, g->dz, &ctx->coefs);
@@ -305,20 +306,11 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
     ctx->wavelet.assign(m->wavelet, m->wavelet + g->nt);
     // sparse source: every non-zero sample (CPU_function.c:326-338 adds all)
     std::vector<SrcEntry> fused, band, all;
-    if (m->source) {
-        const float *s = m->source;
-        for (int z = 0; z < g->nz; ++z)
-            for (int x = 0; x < g->nx; ++x) {
-                const float *row = s + ((size_t)z * g->nx + x) * g->ny;
-                for (int y = 0; y < g->ny; ++y)
-                    if (row[y] != 0.0f) {
-                        SrcEntry e{x, y, z, row[y]};
-                        all.push_back(e);
-                        bool inside = x >= kRadius && x < g->nx - kRadius && y >= kRadius &&
-                                      y < g->ny - kRadius && z >= kRadius && z < g->nz - kRadius;
-                        (inside ? fused : band).push_back(e);
-                    }
-            }
+    if (m->source) scan_source_volume(m->source, g->nx, g->ny, g->nz, all);
+    for (const SrcEntry &e : all) {
+        const bool inside = e.x >= kRadius && e.x < g->nx - kRadius && e.y >= kRadius &&
+                            e.y < g->ny - kRadius && e.z >= kRadius && e.z < g->nz - kRadius;
+        (inside ? fused : band).push_back(e);
     }
     if (ctx->src_fused) cudaFree(ctx->src_fused);
     if (ctx->src_band) cudaFree(ctx->src_band);

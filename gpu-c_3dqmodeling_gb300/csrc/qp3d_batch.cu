@@ -143,13 +143,6 @@ int tile_height(int nx, int rows)
     return (ncx + ntx - 1) / ntx;
 }
 
-int upload_vol(qp3d_ctx *ctx, const Plan &s, float *dst, const float *src)
-{
-    CK(cudaMemcpy2DAsync(dst, (size_t)s.ldy * 4, src, (size_t)s.g.ny * 4, (size_t)s.g.ny * 4,
-                         (size_t)s.g.nx * s.g.nz, cudaMemcpyHostToDevice, ctx->stream));
-    return QP3D_OK;
-}
-
 int make_tmap(qp3d_ctx *ctx, const Plan &s, float *base, int tile_x, CUtensorMap *tm)
 {
     cuuint64_t dims[3] = {(cuuint64_t)s.g.ny, (cuuint64_t)s.g.nx, (cuuint64_t)s.g.nz};
@@ -337,13 +330,19 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
         d.err = ctx->errword;
         nt_max = std::max(nt_max, P.g.nt);
         CK(cudaMemsetAsync(static_cast<char *>(B->arena) + start, 0, zero_bytes, ctx->stream));
-        if ((rc = upload_vol(ctx, P, const_cast<float *>(d.K), m.vp)) ||
-            (rc = upload_vol(ctx, P, const_cast<float *>(d.E2), m.epsilon)) ||
-            (rc = upload_vol(ctx, P, const_cast<float *>(d.R8), m.delta)))
-            return rc;
-        CKL(launch_params(nullptr, nullptr, nullptr, const_cast<float *>(d.K),
-                          const_cast<float *>(d.E2), const_cast<float *>(d.R8), P.vol, P.g.dt,
-                          ctx->stream));
+        // vp, eps, delta in one piece each to the wavefield buffers (staging,
+        // zeroed again after), then the per-cell parameters, pitched
+        {
+            const float *src[3] = {m.vp, m.epsilon, m.delta};
+            const size_t dense = (size_t)P.g.nx * P.g.ny * P.g.nz * sizeof(float);
+            for (int i = 0; i < 3; ++i)
+                CK(cudaMemcpyAsync(d.U[i], src[i], dense, cudaMemcpyHostToDevice, ctx->stream));
+            CKL(launch_params_dense(d.U[0], d.U[1], d.U[2], const_cast<float *>(d.K),
+                                    const_cast<float *>(d.E2), const_cast<float *>(d.R8),
+                                    P.g.nx, P.g.ny, P.g.nz, P.ldy, P.g.dt, ctx->stream));
+            for (int i = 0; i < 3; ++i)
+                CK(cudaMemsetAsync(d.U[i], 0, (size_t)P.vol * sizeof(float), ctx->stream));
+        }
         static const float first[kSpecHist] = {1.0f};   // no prediction yet
         CK(cudaMemcpyAsync(d.spec_err, first, sizeof(first), cudaMemcpyHostToDevice,
                            ctx->stream));
@@ -556,20 +555,14 @@ extern "C" int qp3d_batch(qp3d_ctx *ctx, int nshots, const qp3d_shot *shots)
         P.hy = g.ny - 2 * g.pml;
         bool band = false;
         if (m.source) {
-            const float *s = m.source;
-            for (int z = 0; z < g.nz; ++z)
-                for (int x = 0; x < g.nx; ++x) {
-                    const float *row = s + ((size_t)z * g.nx + x) * g.ny;
-                    for (int y = 0; y < g.ny; ++y)
-                        if (row[y] != 0.0f) {
-                            const bool inside = x >= kRadius && x < g.nx - kRadius &&
-                                                y >= kRadius && y < g.ny - kRadius &&
-                                                z >= kRadius && z < g.nz - kRadius;
-                            if (!inside) band = true;
-                            else if (P.src.size() <= (size_t)kMaxFusedSources)
-                                P.src.push_back(SrcEntry{x, y, z, row[y]});
-                        }
-                }
+            std::vector<SrcEntry> all;
+            scan_source_volume(m.source, g.nx, g.ny, g.nz, all);
+            for (const SrcEntry &e : all) {
+                const bool inside = e.x >= kRadius && e.x < g.nx - kRadius && e.y >= kRadius &&
+                                    e.y < g.ny - kRadius && e.z >= kRadius && e.z < g.nz - kRadius;
+                if (!inside) band = true;
+                else if (P.src.size() <= (size_t)kMaxFusedSources) P.src.push_back(e);
+            }
         }
         derive_coefs(m.c, m.c2, g.dx, g.dy, g.dz, &coefs[i]);
         Carver cv{nullptr};

@@ -14,9 +14,36 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace qp3d {
+
+// The reference adds the whole source volume every step
+// (CPU_function.c:326-338); its non-zero samples are the sparse source.
+// Planes are split over up to 16 threads and the lists joined in plane
+// order, so the order is that of one sequential scan.
+void scan_source_volume(const float *s, int nx, int ny, int nz, std::vector<SrcEntry> &out)
+{
+    out.clear();
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nth = (int)std::max(1u, std::min(16u, hw ? hw : 1u));
+    std::vector<std::vector<SrcEntry>> part(nth);
+    auto work = [&](int t) {
+        const int z0 = (int)((long long)nz * t / nth), z1 = (int)((long long)nz * (t + 1) / nth);
+        for (int z = z0; z < z1; ++z)
+            for (int x = 0; x < nx; ++x) {
+                const float *row = s + ((size_t)z * nx + x) * ny;
+                for (int y = 0; y < ny; ++y)
+                    if (row[y] != 0.0f) part[t].push_back(SrcEntry{x, y, z, row[y]});
+            }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nth; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto &t : th) t.join();
+    for (auto &p : part) out.insert(out.end(), p.begin(), p.end());
+}
 
 // FD tables with the 1/h factors folded in.  The reference divides every tap
 // by dx (first derivative, CPU_function.c:314-316) or dx*dx (second,

@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace qp3d {
 
 constexpr int kRadius = 5;        // 10th-order stencil (M/2 with M = 10)
@@ -218,11 +220,18 @@ cudaError_t launch_record(const float *u, float *rec, int nx, int ny, int pml,
 cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0,
                         int y1, int z0, int z1, int ldy, long long plane,
                         cudaStream_t stream);
-cudaError_t launch_params(const float *vp, const float *eps, const float *del,
-                          float *K, float *E2, float *R8, long long n, float dt,
-                          cudaStream_t stream);
-// vp, eps, delta (pitched FP32) -> IEEE half, round to nearest even
-cudaError_t launch_to_half(const float *a, __half *h, long long n, cudaStream_t stream);
+// Per-cell parameters (vp dt)^2, 2 eps, 8 (eps - delta), or vp, eps, delta as
+// IEEE half (round to nearest even), from dense [nz][nx][ny] volumes (the
+// caller's layout, copied to the device in one piece) into the pitched
+// layout, row padding zero.
+cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *K,
+                                float *E2, float *R8, int nx, int ny, int nz, int ldy, float dt,
+                                cudaStream_t stream);
+cudaError_t launch_to_half_dense(const float *a, __half *h, int nx, int ny, int nz, int ldy,
+                                 cudaStream_t stream);
+// Every non-zero sample of a dense [nz][nx][ny] source volume, in index order
+// (z, then x, then y), scanned by several host threads.
+void scan_source_volume(const float *s, int nx, int ny, int nz, std::vector<SrcEntry> &out);
 // Dynamic shared memory of a plane kernel; nsrc = fused sources of the shot
 // (the per-CTA source list has room for all of them).
 size_t plane_smem_bytes(int tile_x, int pml, int nsrc = kMaxFusedSources);

@@ -856,7 +856,7 @@ __device__ __forceinline__ float2 aniso_s2(float2 h2, float2 m2, float2 v2, floa
 // CTA; the batched kernel runs many per CTA (REUSE: barriers invalidated at
 // the end, return value uniform over the CTA; false = a wait timed out).
 // Per-cell parameters of a quad from half-precision vp, eps, delta, with the
-// operations of qp3d_params_kernel: (vp dt)^2, 2 eps, 8 (eps - delta).
+// operations of qp3d_params_dense_kernel: (vp dt)^2, 2 eps, 8 (eps - delta).
 __device__ __forceinline__ void quad_params_half(const PlaneParams &p, uint2 hv, uint2 he,
                                                  uint2 hd, float4 &K, float4 &E2, float4 &R8)
 {
@@ -1350,17 +1350,40 @@ __global__ void qp3d_crop_kernel(const float *u, float *out, int x0, int x1, int
     }
 }
 
-// Per-cell parameters from vp, eps, delta (in place: K holds vp, E2 holds
-// eps, R8 holds delta on entry).
-__global__ void qp3d_params_kernel(float *K, float *E2, float *R8, long long n, float dt)
+// Per-cell parameters (vp dt)^2, 2 eps, 8 (eps - delta) from dense
+// [nz][nx][ny] volumes (the caller's layout) into the pitched layout, one
+// thread per pitched cell, row padding zero; and the same layout change for
+// half-precision storage.
+__global__ void qp3d_params_dense_kernel(const float *vp, const float *eps, const float *del,
+                                         float *K, float *E2, float *R8, int ny,
+                                         long long vol, int ldy, float dt)
 {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
          i += (long long)gridDim.x * blockDim.x) {
-        float vdt = __fmul_rn(K[i], dt);
-        float e = E2[i], d = R8[i];
-        K[i] = __fmul_rn(vdt, vdt);
-        E2[i] = __fmul_rn(2.0f, e);
-        R8[i] = __fmul_rn(8.0f, __fsub_rn(e, d));
+        const long long row = i / ldy;
+        const int y = (int)(i - row * ldy);
+        float k = 0.0f, e2 = 0.0f, r8 = 0.0f;
+        if (y < ny) {
+            const long long j = row * ny + y;
+            const float vdt = __fmul_rn(vp[j], dt), e = eps[j], d = del[j];
+            k = __fmul_rn(vdt, vdt);
+            e2 = __fmul_rn(2.0f, e);
+            r8 = __fmul_rn(8.0f, __fsub_rn(e, d));
+        }
+        K[i] = k;
+        E2[i] = e2;
+        R8[i] = r8;
+    }
+}
+
+__global__ void qp3d_to_half_dense_kernel(const float *a, __half *h, int ny, long long vol,
+                                          int ldy)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long row = i / ldy;
+        const int y = (int)(i - row * ldy);
+        h[i] = __float2half_rn(y < ny ? a[row * ny + y] : 0.0f);
     }
 }
 
@@ -1865,13 +1888,6 @@ __global__ void qp3d_from_bf16_kernel(const __nv_bfloat16 *h, float *a, long lon
         a[i] = __bfloat162float(h[i]);
 }
 
-__global__ void qp3d_to_half_kernel(const float *a, __half *h, long long n)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x)
-        h[i] = __float2half_rn(a[i]);
-}
-
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
@@ -2086,21 +2102,24 @@ cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_to_half(const float *a, __half *h, long long n, cudaStream_t stream)
+cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *K,
+                                float *E2, float *R8, int nx, int ny, int nz, int ldy, float dt,
+                                cudaStream_t stream)
 {
-    if (n <= 0) return cudaSuccess;
-    long long b = (n + 255) / 256;
-    qp3d_to_half_kernel<<<(int)(b > 8192 ? 8192 : b), 256, 0, stream>>>(a, h, n);
+    const long long vol = (long long)nz * nx * ldy;
+    const long long b = (vol + 255) / 256;
+    qp3d_params_dense_kernel<<<(int)(b > 16384 ? 16384 : b), 256, 0, stream>>>(
+        vp, eps, del, K, E2, R8, ny, vol, ldy, dt);
     return cudaGetLastError();
 }
 
-cudaError_t launch_params(const float * /*vp*/, const float * /*eps*/, const float * /*del*/,
-                          float *K, float *E2, float *R8, long long n, float dt,
-                          cudaStream_t stream)
+cudaError_t launch_to_half_dense(const float *a, __half *h, int nx, int ny, int nz, int ldy,
+                                 cudaStream_t stream)
 {
-    long long b = (n + 255) / 256;
-    int blocks = (int)(b > 8192 ? 8192 : b);
-    qp3d_params_kernel<<<blocks, 256, 0, stream>>>(K, E2, R8, n, dt);
+    const long long vol = (long long)nz * nx * ldy;
+    const long long b = (vol + 255) / 256;
+    qp3d_to_half_dense_kernel<<<(int)(b > 16384 ? 16384 : b), 256, 0, stream>>>(a, h, ny, vol,
+                                                                                ldy);
     return cudaGetLastError();
 }
 
