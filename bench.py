@@ -488,7 +488,7 @@ def run_batch_arm(args, dist):
                        "shots": len(shots), "nt": nt, "cells_total": sum(cells),
                        "cells_mean": round(sum(cells) / len(cells)),
                        "l2": "inputs larger than L2 (working set %.0f GB)" %
-                             (sum(21 * c * 4 for c in cells) / 1e9),
+                             (sum(17 * c * 4 for c in cells) / 1e9),
                        "parallelism": "replicas" if dist.world > 1 else "single"},
             "gcell_per_s": round(dist.world * work * args.steps / (run_ms / 1e3) / 1e9, 3),
             "step_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
