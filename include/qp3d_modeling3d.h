@@ -13,7 +13,10 @@
  *   - with snapflag == 1, every ntsnap steps it writes <snap_file><k>.dat
  *     (interior volume) and <snap_file>_xz/_yz/_xy<k>.dat slices.
  * Runs on CUDA device 0 like the reference.  It has no return value; errors
- * are reported on stderr (use qp3d_forward for status codes).
+ * are reported on stderr (use qp3d_forward for status codes).  Like the
+ * reference it is not re-entrant: all calls share one library context that
+ * keeps the device buffers between calls of the same grid size; call it from
+ * one host thread at a time.
  */
 #ifndef QP3D_MODELING3D_H
 #define QP3D_MODELING3D_H
