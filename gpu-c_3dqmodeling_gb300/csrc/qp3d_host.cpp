@@ -39,9 +39,14 @@ void scan_source_volume(const float *s, int nx, int ny, int nz, std::vector<SrcE
             }
     };
     std::vector<std::thread> th;
-    for (int t = 1; t < nth; ++t) th.emplace_back(work, t);
+    int started = 1;
+    try {
+        for (int t = 1; t < nth; ++t, ++started) th.emplace_back(work, t);
+    } catch (...) {   // no more threads: this one scans the rest
+    }
     work(0);
     for (auto &t : th) t.join();
+    for (int t = started; t < nth; ++t) work(t);
     for (auto &p : part) out.insert(out.end(), p.begin(), p.end());
 }
 

@@ -190,3 +190,55 @@ int main(void)
     assert out.returncode == 0
     rc = int(out.stdout.split()[0])
     assert rc in (0, -2)   # QP3D_OK on a GPU machine, QP3D_ERR_CUDA without one
+
+
+def test_source_scan_matches_a_sequential_scan(tmp_path):
+    """The threaded scan of the source volume (qp3d::scan_source_volume, used
+    by qp3d_shot_load and qp3d_batch) returns every non-zero sample in the
+    order of one sequential z, x, y scan."""
+    src = tmp_path / "scan.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+#include "qp3d_internal.h"
+int main()
+{
+    const int nx = 37, ny = 29, nz = 53;
+    std::vector<float> v((size_t)nx * ny * nz, 0.0f);
+    unsigned s = 12345u;
+    for (size_t i = 0; i < v.size(); ++i) {
+        s = s * 1664525u + 1013904223u;
+        if ((s >> 24) < 3) v[i] = (float)(s & 0xffff) - 30000.0f;   /* ~1% non-zero */
+    }
+    std::vector<qp3d::SrcEntry> got;
+    qp3d::scan_source_volume(v.data(), nx, ny, nz, got);
+    size_t k = 0;
+    for (int z = 0; z < nz; ++z)
+        for (int x = 0; x < nx; ++x)
+            for (int y = 0; y < ny; ++y) {
+                const float f = v[((size_t)z * nx + x) * ny + y];
+                if (f == 0.0f) continue;
+                if (k >= got.size() || got[k].x != x || got[k].y != y || got[k].z != z ||
+                    got[k].v != f) {
+                    printf("mismatch at %zu\n", k);
+                    return 1;
+                }
+                ++k;
+            }
+    printf("%zu %zu\n", k, got.size());
+    return k == got.size() ? 0 : 1;
+}
+''')
+    lib_dir = os.path.dirname(qp3d.LIB_PATH)
+    exe = str(tmp_path / "scan")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "gpu-c_3dqmodeling_gb300",
+                                                                     "csrc"),
+                        "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include",
+                        str(src), "-o", exe, "-L" + lib_dir, "-lqp3d", "-Wl,-rpath," + lib_dir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout
+    n, m = (int(t) for t in out.stdout.split())
+    assert n == m and n > 100
