@@ -84,6 +84,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="scale the horizontal/vertical extent (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip the reference GPU kernels' sample")
     ap.add_argument("--workload", default="single",
                     choices=["single", "batch", "large", "adjoint"])
     ap.add_argument("--shots", type=int, default=64,
@@ -247,9 +249,64 @@ def cpu_sample(shot, nsteps, k0=1500, seed=0):
     return time.perf_counter() - t0, threads
 
 
+def repo_native_libs():
+    """Shared objects of this repository mapped into the process (Linux)."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if line.strip() else ""
+                if path.endswith(".so") and path.startswith(ROOT):
+                    out.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
+def reference_gpu_sample(shot, steps_dev=10, steps_host=3, seed=0):
+    """The reference's own GPU kernels (GPU_kernel.cu compiled for sm_103a)
+    in its driver's step sequence on cuda:0, from a dense random state: Gcell/s
+    with the step max taken on the device, and as the reference's driver does
+    it (full D2H copies of ux, uy, uz and u2 every step, host scan)."""
+    from oracle import oracle as O
+    import synthetic
+    if not O.ref_gpu_available():
+        return {"unavailable": "reference GPU kernels were not compiled (no checkout)"}
+    try:
+        prob = shot.to_oracle(O)
+        u_prev, u_cur, pml = synthetic.random_state(shot, seed=seed)
+        out = {"kind": "reference", "source": "GPU_kernel.cu unmodified, nvcc -cubin sm_103a",
+               "unit": "Gcell/s", "workload": WORKLOAD_NAME}
+        for key, n, host in (("device_max", steps_dev, False), ("host_max", steps_host, True)):
+            st = O.State(prob)
+            st.u1[:] = u_prev
+            st.u2[:] = u_cur
+            st.u3[:] = u_cur
+            st.pml[:] = pml
+            k0 = max(0, min(1500, shot.nt - n))
+            O.run_reference_gpu(prob, k0=k0, nsteps=1, state=st.copy(), host_max=host,
+                                want_record=False)   # warm-up (module load, first launches)
+            _, _, _, ms = O.run_reference_gpu(prob, k0=k0, nsteps=n, state=st, host_max=host,
+                                              want_record=False)
+            out[key] = {"value": round(shot.N * n / (ms * 1e-3) / 1e9, 4), "steps": n,
+                        "ms_per_step": round(ms / n, 3)}
+        out["device_max"]["form"] = ("grad, scalar_operator, wavefield_update, addsource, "
+                                     "exchange per step; max by a device reduction; record "
+                                     "plane copied to the host")
+        out["host_max"]["form"] = ("as 3dPureqPModeling_single_shot.cu:282-337: ux, uy, uz "
+                                   "and u2 copied to the host every step, max scanned there")
+        return out
+    except Exception as e:   # no usable GPU in this process
+        return {"unavailable": str(e).splitlines()[0][:200]}
+
+
 def run_reference_arm(args, dist):
     if dist.rank != 0:
         return 0
+    import synthetic
+    # inputs from the oracle's restatements of the host utilities: this
+    # process must not load the library it is compared with
+    synthetic.set_backend("oracle")
     w = workload(args)
     shot = make_shot(w)
     cells = shot.N
@@ -275,7 +332,11 @@ def run_reference_arm(args, dist):
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "native_libs": repo_native_libs(),
     }
+    if not args.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu_sample(shot)
+        line["native_libs"] = repo_native_libs()
     print(json.dumps(line), flush=True)
     return 0
 

@@ -6,32 +6,73 @@ Inputs are built exactly as the reference's main program builds them
 (3dPureqPModeling1.0.c:234-268): interior model -> extend_model into the PML
 shell -> vpmax = (1 + 2 max eps) max vp -> pmlcoff -> Source at the window
 centre on the top of the interior, receivers on that plane.
+
+The host utilities (extend_model, pmlcoff, Source, FD tables) come from the
+library by default.  set_backend("oracle") takes them from the CPU oracle
+instead and returns oracle problems: the CPU reference measurement builds its
+inputs that way, so that its process never loads the library it is compared
+with.  Both restate the same reference functions and give identical inputs.
 """
 import numpy as np
 
-import qp3d
+_BACKEND = "qp3d"
+
+
+def set_backend(name):
+    """'qp3d' (default) or 'oracle' (see the module docstring)."""
+    global _BACKEND
+    if name not in ("qp3d", "oracle"):
+        raise ValueError("unknown backend %r" % (name,))
+    _BACKEND = name
+
+
+class _OracleHost:
+    """The oracle's restatements under the library's names."""
+
+    def __init__(self):
+        from oracle import oracle as O
+        self.extend_model = O.extend_model
+        self.pmlcoff = O.pmlcoff
+        self.source = O.source
+        self.fdcoff = O.fdcoff
+        self.pml_state_size = O.pml_state_size
+        self.Shot = O.Problem
+
+    @staticmethod
+    def absmax(a):
+        # CPU_function.c:10-22 starts at 0 and keeps the largest |a|
+        a = np.asarray(a, np.float32)
+        return float(np.max(np.abs(a))) if a.size else 0.0
+
+
+def _host():
+    if _BACKEND == "oracle":
+        return _OracleHost()
+    import qp3d
+    return qp3d
 
 
 def _finish(vp_i, eps_i, del_i, pml, dx, dt, nt, fm, src_xyz=None, sz=None, amp=1.0,
             alpha=1.0):
+    h = _host()
     nz0, hx, hy = vp_i.shape
     nx, ny, nz = hx + 2 * pml, hy + 2 * pml, nz0 + 2 * pml
-    vp = qp3d.extend_model(vp_i, nx, ny, nz, pml)
-    eps = qp3d.extend_model(eps_i, nx, ny, nz, pml)
-    dl = qp3d.extend_model(del_i, nx, ny, nz, pml)
+    vp = h.extend_model(vp_i, nx, ny, nz, pml)
+    eps = h.extend_model(eps_i, nx, ny, nz, pml)
+    dl = h.extend_model(del_i, nx, ny, nz, pml)
     # float arithmetic throughout, as 3dPureqPModeling.c:227 computes vpmax
-    vpmax = (np.float32(1) + np.float32(2) * np.float32(qp3d.absmax(eps))) * \
-        np.float32(qp3d.absmax(vp))
-    prof = qp3d.pmlcoff(pml, float(vpmax), dx, dx, dx)
+    vpmax = (np.float32(1) + np.float32(2) * np.float32(h.absmax(eps))) * \
+        np.float32(h.absmax(vp))
+    prof = h.pmlcoff(pml, float(vpmax), dx, dx, dx)
     if src_xyz is None:   # 3dPureqPModeling1.0.c:263-265
         src_xyz = ((hx - 1) // 2, (hy - 1) // 2, 0)
     sx, sy, sz0 = (v + pml for v in src_xyz)
-    src, wav = qp3d.source(sx, sy, sz0, fm, amp, alpha, dt, dx, dx, dx, 1.0 / fm, nt,
-                           nx, ny, nz)
-    c, c2 = qp3d.fdcoff()
+    src, wav = h.source(sx, sy, sz0, fm, amp, alpha, dt, dx, dx, dx, 1.0 / fm, nt,
+                        nx, ny, nz)
+    c, c2 = h.fdcoff()
     if sz is None:
         sz = sz0
-    return qp3d.Shot(nx, ny, nz, pml, sz, dx, dx, dx, dt, vp, eps, dl, src, wav, prof, c, c2)
+    return h.Shot(nx, ny, nz, pml, sz, dx, dx, dx, dt, vp, eps, dl, src, wav, prof, c, c2)
 
 
 def linear_vti(h=100, nz0=100, pml=20, nt=1000, dx=10.0, dt=5e-4, fm=25.0, src=(50, 50, 5),
@@ -189,6 +230,6 @@ def random_state(shot, seed=0, amp=1e-3):
             np.float32)
         return v.ravel()
     u_prev, u_cur = vol(), vol()
-    n = qp3d.pml_state_size(nx, ny, nz, pml)
+    n = _host().pml_state_size(nx, ny, nz, pml)
     pml_state = (amp * rng.standard_normal(n + 1)).astype(np.float32)
     return u_prev, u_cur, pml_state

@@ -160,6 +160,10 @@ class Problem:
     def nt(self):
         return len(self.wavelet)
 
+    def to_oracle(self, O=None):
+        """Already an oracle problem (the library's Shot converts itself)."""
+        return self
+
     def args(self, nthreads=0):
         a = OracleArgs()
         a.nx, a.ny, a.nz, a.pml, a.sz = self.nx, self.ny, self.nz, self.pml, self.sz
@@ -231,6 +235,64 @@ def run_reference(prob, k0=0, nsteps=None, state=None):
     if rc != 0:
         raise RuntimeError("ref_run failed: %d" % rc)
     return rec, mx, state
+
+
+_refgpu = None
+
+
+def ref_gpu_available():
+    """True when the reference GPU kernels were compiled (a cubin exists)."""
+    return os.path.exists(_build.REF_CUBIN)
+
+
+def ref_gpu_lib():
+    """Host driver of the reference's own GPU kernels (ref_gpu.cu), with the
+    reference cubin loaded; None when the cubin was not built."""
+    global _refgpu
+    if _refgpu is None:
+        if not ref_gpu_available():
+            return None
+        _build.build_reference_gpu()
+        L = ctypes.CDLL(_build.REFGPU_LIB)
+        L.refgpu_load.restype = ctypes.c_int
+        L.refgpu_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.refgpu_run.restype = ctypes.c_int
+        L.refgpu_run.argtypes = ([ctypes.POINTER(OracleArgs), ctypes.c_int, ctypes.c_int] +
+                                 [ctypes.c_void_p] * 6 + [ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_double), ctypes.c_char_p,
+                                 ctypes.c_size_t])
+        err = ctypes.create_string_buffer(512)
+        if L.refgpu_load(_build.REF_CUBIN.encode(), err, len(err)) != 0:
+            raise RuntimeError("reference GPU kernels: " + err.value.decode())
+        _refgpu = L
+    return _refgpu
+
+
+def run_reference_gpu(prob, k0=0, nsteps=None, state=None, host_max=False, want_record=True):
+    """The reference's own GPU kernels (GPU_kernel.cu built for sm_103a) on
+    cuda:0, in the reference GPU driver's step sequence; returns (record,
+    uxyzmax, state, ms) with ms the wall time of the time loop.  host_max:
+    take each step's max on the host from full copies, as the reference's
+    driver does, instead of a device reduction (same values)."""
+    L = ref_gpu_lib()
+    if L is None:
+        raise RuntimeError("reference GPU kernels were not built")
+    if nsteps is None:
+        nsteps = prob.nt - k0
+    if state is None:
+        state = State(prob, np.float32)
+    hx, hy = prob.nx - 2 * prob.pml, prob.ny - 2 * prob.pml
+    rec = np.zeros((nsteps, hx, hy), np.float32) if want_record else None
+    mx = np.zeros(nsteps, np.float32)
+    ms = ctypes.c_double(0.0)
+    err = ctypes.create_string_buffer(512)
+    args = prob.args()
+    rc = L.refgpu_run(ctypes.byref(args), k0, nsteps, _ptr(state.u1), _ptr(state.u2),
+                      _ptr(state.u3), _ptr(state.pml), _ptr(rec), _ptr(mx), int(host_max),
+                      ctypes.byref(ms), err, len(err))
+    if rc != 0:
+        raise RuntimeError("refgpu_run failed: " + err.value.decode())
+    return rec, mx, state, ms.value
 
 
 # ---------------------------------------------------------------------------

@@ -37,3 +37,21 @@ def bits_equal(a, b):
     a = np.ascontiguousarray(a, np.float32)
     b = np.ascontiguousarray(b, np.float32)
     return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+_PLAIN = {}
+
+
+def plain_shot_oracles(shot):
+    """(REF32 record, FP64 record) of a whole shot, computed once per test
+    session for a given shot geometry and model (the 1000-step plain shot is
+    compared in several tests)."""
+    from oracle import oracle as O
+    key = (shot.nx, shot.ny, shot.nz, shot.pml, shot.nt, shot.sz,
+           float(np.asarray(shot.vp, np.float64).sum()), float(np.asarray(shot.eps).sum()))
+    if key not in _PLAIN:
+        prob = shot.to_oracle(O)
+        r32, _, _ = O.run(O.REF32, prob)
+        r64, _, _ = O.run(O.F64, prob)
+        _PLAIN[key] = (r32, r64)
+    return _PLAIN[key]

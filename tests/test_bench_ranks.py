@@ -25,3 +25,23 @@ def test_reference_arm_two_ranks(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # the CPU reference never loads the library it is compared with
+    assert d["native_libs"] and all(l.startswith("oracle") for l in d["native_libs"]), d
+
+
+def test_reference_inputs_match_library_inputs():
+    """The oracle backend of the workload generator builds the same inputs
+    as the library's host utilities, bit for bit."""
+    import numpy as np
+    import synthetic
+    a = synthetic.small_case(nt=30, seed=5)
+    synthetic.set_backend("oracle")
+    try:
+        b = synthetic.small_case(nt=30, seed=5)
+    finally:
+        synthetic.set_backend("qp3d")
+    assert type(b).__module__.endswith("oracle")
+    for x, y in [(a.vp, b.vp), (a.eps, b.eps), (a.delta, b.delta), (a.src, b.src),
+                 (a.wavelet, b.wavelet), (a.c, b.c), (a.c2, b.c2)] + list(zip(a.prof, b.prof)):
+        assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32))
+    assert (a.nx, a.ny, a.nz, a.pml, a.sz) == (b.nx, b.ny, b.nz, b.pml, b.sz)

@@ -18,7 +18,7 @@ import pytest
 import qp3d
 import synthetic
 from oracle import oracle as O
-from helpers import FIXTURES, bits_equal, load_fixture, max_abs_rel_peak, rel_l2
+from helpers import FIXTURES, bits_equal, load_fixture, max_abs_rel_peak, plain_shot_oracles, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -156,9 +156,7 @@ def test_linear_vti_plain_shot_full(ctx):
     S-threshold flips dominate; the first 500 steps hold 1e-5."""
     shot = synthetic.linear_vti()
     rec = ctx.forward(shot)
-    prob = shot.to_oracle(O)
-    r32, _, _ = O.run(O.REF32, prob)
-    r64, _, _ = O.run(O.F64, prob)
+    r32, r64 = plain_shot_oracles(shot)
     e_rel, e_max = rel_l2(rec, r32), max_abs_rel_peak(rec, r32)
     e_half = rel_l2(rec[:500], r32[:500])
     e64, e64_ref = rel_l2(rec, r64), rel_l2(r32, r64)
