@@ -36,7 +36,7 @@ SOURCES = [
 ]
 MAIN = ("qp3d_main.cpp", ["g++", "-O2", "-std=c++17", "-Wall", "-I", INCLUDE])
 EXE = os.path.join(HERE, "bin", "qp3d_modeling")
-HEADERS = ["qp3d_internal.h"]
+HEADERS = ["qp3d_internal.h", "qp3d_exact.h", "qp3d_ctx.h"]
 
 
 def _newer(target, deps):

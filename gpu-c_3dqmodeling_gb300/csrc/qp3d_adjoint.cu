@@ -206,7 +206,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     memset(&a, 0, sizeof(a));
     a.nx = g->nx; a.ny = g->ny; a.nz = g->nz; a.ldy = ctx->ldy; a.pml = g->pml; a.sz = g->sz;
     a.hx = ctx->hx; a.hy = ctx->hy; a.plane = ctx->plane; a.k = ctx->coefs; a.dt = g->dt;
-    a.K = ctx->K; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers;
+    a.VP = ctx->VP; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers;
     for (int c = (keep ? 1 : nck) - 1; c >= 0; --c) {
         const int k0 = c * C, k1 = std::min(nt, k0 + C);
         if (!keep) {   // restore the checkpoint, recompute keeping u^k

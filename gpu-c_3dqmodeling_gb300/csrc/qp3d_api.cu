@@ -41,7 +41,7 @@ extern "C" const char *qp3d_ctx_last_error(const qp3d_ctx *ctx) { return ctx ? c
 static void free_shot(qp3d_ctx *ctx)
 {
     cudaSetDevice(ctx->device);
-    float **bufs[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->K,     &ctx->E2,
+    float **bufs[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->VP,     &ctx->E2,
                       &ctx->R8,    &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0],
                       &ctx->W3[1], &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],
                       &ctx->W21[0], &ctx->W21[1], &ctx->record, &ctx->gmax, &ctx->snap_dev,
@@ -239,7 +239,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         float **vols[] = {&ctx->U[0],  &ctx->U[1],  &ctx->U[2],  &ctx->W1[0], &ctx->W1[1],
                           &ctx->W1[2], &ctx->W3[0], &ctx->W3[1], &ctx->W3[2], &ctx->P[0],
                           &ctx->P[1],  &ctx->P[2],  &ctx->W21[0], &ctx->W21[1],
-                          &ctx->K,     &ctx->E2,    &ctx->R8};
+                          &ctx->VP,     &ctx->E2,    &ctx->R8};
         const int nvols = half ? 14 : 17;   // half storage: no FP32 parameter volumes
         for (int v = 0; v < nvols; ++v)
             if ((rc = alloc_vol(ctx, vols[v]))) {
@@ -288,7 +288,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
                 CKL(launch_to_half_dense(ctx->U[i], dst[i], g->nx, g->ny, g->nz, ctx->ldy,
                                          ctx->stream));
         } else {
-            CKL(launch_params_dense(ctx->U[0], ctx->U[1], ctx->U[2], ctx->K, ctx->E2, ctx->R8,
+            CKL(launch_params_dense(ctx->U[0], ctx->U[1], ctx->U[2], ctx->VP, ctx->E2, ctx->R8,
                                     g->nx, g->ny, g->nz, ctx->ldy, g->dt, ctx->stream));
         }
     }
@@ -402,7 +402,7 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.u_cur = ctx->U[a];
     p.u_prev = ctx->U[b];
     p.u_out = ctx->U[c];
-    p.prm_k = ctx->K; p.prm_e = ctx->E2; p.prm_r = ctx->R8;
+    p.prm_v = ctx->VP; p.prm_e = ctx->E2; p.prm_r = ctx->R8;
     p.h_vp = ctx->h_vp; p.h_eps = ctx->h_eps; p.h_del = ctx->h_del;
     p.half_params = ctx->half_loaded ? 1 : 0;
     const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
@@ -412,6 +412,7 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.w21o = ctx->W21[k % 2];
     p.w21n = ctx->W21[(k + 1) % 2];
     p.layers = ctx->layers;
+    p.arith = ctx->arith;
     p.gmax = ctx->gmax;
     float *rec_plane = ctx->record + (size_t)k * ctx->hx * ctx->hy;
     p.record = ctx->rec_fused ? rec_plane : nullptr;
@@ -860,6 +861,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "spec_bias_ppm") && value >= -500000 && value <= 1000000)
         ctx->spec_bias = value * 1e-6f;
     else if (!strcmp(key, "param_fp16") && (value == 0 || value == 1)) ctx->param_fp16 = value;
+    else if (!strcmp(key, "arith") && (value == kArithRef || value == kArithFast)) ctx->arith = value;
     else if (!strcmp(key, "adj_ckpt_bf16") && (value == 0 || value == 1)) ctx->adj_bf16 = value;
     else if (!strcmp(key, "adj_keep_all") && value >= -1 && value <= 1) ctx->adj_keep = value;
     else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
@@ -884,6 +886,7 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "spec_delta_ppm")) return (int)(ctx->delta_min * 1e6f + 0.5f);
     if (!strcmp(key, "spec_bias_ppm")) return (int)lrintf(ctx->spec_bias * 1e6f);
     if (!strcmp(key, "param_fp16")) return ctx->param_fp16;
+    if (!strcmp(key, "arith")) return ctx->arith;
     if (!strcmp(key, "adj_ckpt_bf16")) return ctx->adj_bf16;
     if (!strcmp(key, "adj_keep_all")) return ctx->adj_keep;
     if (!strcmp(key, "batch_graph")) return ctx->batch_graph;

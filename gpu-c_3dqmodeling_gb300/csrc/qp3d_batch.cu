@@ -122,7 +122,7 @@ void carve(Plan &s, Carver &c, size_t *zero_bytes)
     d.sres = c.take<float>(2 * nt);
     d.amask = c.take<unsigned>((size_t)defer_mask_words((long long)vol));
     if (zero_bytes) *zero_bytes = c.off - start;
-    d.K = c.take<float>(vol);
+    d.VP = c.take<float>(vol);
     d.E2 = c.take<float>(vol);
     d.R8 = c.take<float>(vol);
     d.spec_err = c.take<float>(kSpecHist);
@@ -200,6 +200,7 @@ class Runner {
         a.work = B->d_work[c];
         a.nwork = L[c].nwork;
         a.queue = B->d_ctr + 4 + queue;
+        a.arith = ctx->arith;
         return a;
     }
     int enqueue_step(int c, bool spec);
@@ -255,7 +256,7 @@ int Runner::build_candidate(int c, std::vector<Plan *> &G)
     l.threads = batch_plane_threads(max_tile);
     l.smem = smem;
     int per_sm = 0;
-    CK(batch_ctas_per_sm(2, l.threads, l.smem, &per_sm));
+    CK(batch_ctas_per_sm(2, ctx->arith, l.threads, l.smem, &per_sm));
     if (per_sm < 1) return ctx_fail(ctx, QP3D_ERR_CUDA, "batched step kernel does not fit an SM");
     l.grid = std::max(1, std::min(l.nwork, per_sm * ctx->nsm));
     return QP3D_OK;
@@ -337,7 +338,7 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
             const size_t dense = (size_t)P.g.nx * P.g.ny * P.g.nz * sizeof(float);
             for (int i = 0; i < 3; ++i)
                 CK(cudaMemcpyAsync(d.U[i], src[i], dense, cudaMemcpyHostToDevice, ctx->stream));
-            CKL(launch_params_dense(d.U[0], d.U[1], d.U[2], const_cast<float *>(d.K),
+            CKL(launch_params_dense(d.U[0], d.U[1], d.U[2], const_cast<float *>(d.VP),
                                     const_cast<float *>(d.E2), const_cast<float *>(d.R8),
                                     P.g.nx, P.g.ny, P.g.nz, P.ldy, P.g.dt, ctx->stream));
             for (int i = 0; i < 3; ++i)

@@ -40,7 +40,7 @@ struct qp3d_ctx {
     size_t smem = 0;
     bool rec_fused = true;
     float *U[3] = {nullptr, nullptr, nullptr};
-    float *K = nullptr, *E2 = nullptr, *R8 = nullptr;
+    float *VP = nullptr, *E2 = nullptr, *R8 = nullptr;   // vp, 2 eps, 8 (eps - delta)
     __half *h_vp = nullptr, *h_eps = nullptr, *h_del = nullptr;   // param_fp16 storage
     bool half_loaded = false;        // the loaded shot stores its parameters as half
     float *W1[3] = {}, *W3[3] = {}, *P[3] = {}, *W21[2] = {};
@@ -86,6 +86,9 @@ struct qp3d_ctx {
     bool delta_min_set = false;
     float spec_bias = 0.0f;          // test hook: shifts the predicted window
     int param_fp16 = 0;              // store vp, eps, delta as IEEE half (next load)
+    // arithmetic of the step: the fast folded form (default) or the reference
+    // CPU operators' roundings, bit for bit ("arith" tuning key)
+    int arith = qp3d::kArithFast;
     long long launches = 0;          // kernels launched by this context
     // batched shots (qp3d_batch)
     qp3d::BatchState *batch = nullptr;

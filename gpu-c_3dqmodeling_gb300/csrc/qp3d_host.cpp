@@ -8,6 +8,7 @@
 #include "qp3d.h"
 #include "qp3d_modeling3d.h"
 #include "qp3d_internal.h"
+#include "qp3d_exact.h"
 
 #include <cmath>
 #include <cstdio>
@@ -82,21 +83,28 @@ void derive_coefs(const float *c, const float *c2, float dx, float dy, float dz,
     k->kx2 = make_float2(k->kx, k->kx);
     k->ky2 = make_float2(k->ky, k->ky);
     k->kz2 = make_float2(k->kz, k->kz);
+    // reference arithmetic: the tables as they are, and the divisors
+    for (int m = 0; m < kRadius; m++) {
+        k->rc[m] = make_float2(c[31 + m], c[31 + m]);
+        k->rc2[m] = make_float2(c2[31 + m], c2[31 + m]);
+    }
+    const float h[3] = {dx, dy, dz}, h2[3] = {dx2, dy2, dz2};
+    for (int a = 0; a < 3; a++) {
+        k->rh[a] = h[a];
+        k->rh2[a] = h2[a];
+    }
 }
 
-// Per-layer PML recursion coefficients (GPU_kernel.cu:569-572):
-//   a1 = (d*dt+1)^2 - 3   (the reference squares in double, pow(float,int))
-//   a2 = 2*d*dt - 1,  a3 = 1 - dt*d,  dd = the second profile
+// Per-layer PML recursion coefficients (GPU_kernel.cu:569-572,
+// CPU_function.c:400-404): a1 = (d*dt+1)^2 - 3, which the reference squares
+// in double (pow(float,int)), is exact as the float pair (a1h, a1l); with
+// t = d*dt the other two are a2 = 2*d*dt - 1 = fma(2, t, -1) and
+// a3 = 1 - dt*d = 1 - t; dd is the second profile.  Stored (a1h, a1l, t, dd).
 void derive_layers(const float *d, const float *dd, int pml, float dt, float4 *out)
 {
     for (int i = 0; i < pml; i++) {
-        float b = d[i] * dt + 1.0f;
-        float4 v;
-        v.x = (float)((double)b * (double)b - 3.0);
-        v.y = 2.0f * d[i] * dt - 1.0f;
-        v.z = 1.0f - dt * d[i];
-        v.w = dd[i];
-        out[i] = v;
+        const xr::PmlLayer L = xr::pml_layer(d[i], dd[i], dt);
+        out[i] = make_float4(L.a1h, L.a1l, d[i] * dt, dd[i]);
     }
 }
 

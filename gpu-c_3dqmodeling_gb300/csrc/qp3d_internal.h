@@ -4,7 +4,7 @@
 // so every row starts on a 128-byte boundary):
 //   U[3]            wavefields u(k-1), u(k), u(k+1), rotated by index: a step
 //                   never overwrites its inputs
-//   K, E2, R8       per-cell parameters (vp*dt)^2, 2*eps, 8*(eps-delta)
+//   VP, E2, R8      per-cell parameters vp, 2*eps, 8*(eps-delta)
 //   W1[3],W3[3],P[3] PML split fields, three time levels each, and W21[2],
 //                   rotated by index (no copies).  These are full "shadow"
 //                   volumes: only PML cells are ever touched, so a cell's
@@ -55,7 +55,16 @@ struct Coefs {
     float2 cx2[kRadius], cy2[kRadius], cz2[kRadius];
     float2 c2x2[kRadius], c2y2[kRadius], c2z2[kRadius];
     float2 kx2, ky2, kz2;
+    // Reference arithmetic (qp3d_exact.h): the tables as given (both lanes
+    // alike) and per axis the divisors of the first and second derivatives,
+    // h and h*h rounded.
+    float2 rc[kRadius], rc2[kRadius];                  // c[31+m], c2[31+m]
+    float rh[3], rh2[3];                               // x, y, z
 };
+
+// Arithmetic of the step: the reference CPU operators' roundings
+// (qp3d_exact.h, bit-identical to CPU_function.c) or the folded fast form.
+enum Arith { kArithRef = 0, kArithFast = 1 };
 
 // One source sample: padded coordinates and the amplitude.
 struct SrcEntry {
@@ -83,7 +92,7 @@ struct PlaneParams {
     const float *u_cur;
     const float *u_prev;
     float *u_out;
-    const float *prm_k, *prm_e, *prm_r;
+    const float *prm_v, *prm_e, *prm_r;   // vp, 2 eps, 8 (eps - delta)
     // half-precision parameter storage (half_params != 0): vp, eps, delta as
     // IEEE half, widened in the kernels; prm_* are unused then
     const __half *h_vp, *h_eps, *h_del;
@@ -92,7 +101,10 @@ struct PlaneParams {
     const float *w3o, *w3c; float *w3n;   // w31, w32 -> w33
     const float *po, *pc; float *pn;      // p1, p2 -> p3
     const float *w21o; float *w21n;       // w21 -> w21'
-    const float4 *layers;     // [3][pml] (a1, a2, a3, dd) for lr, fb, tb
+    const float4 *layers;     // [3][pml] (a1h, a1l, d*dt, dd) for lr, fb, tb: the
+                              // reference's a1 = (d*dt+1)^2 - 3 as an exact float
+                              // pair; a2 = 2*d*dt - 1 and a3 = 1 - d*dt follow
+    int arith;                // Arith of this launch
     float *gmax;              // gmax[0..nt): max|grad u| per step
     float *record;            // record plane of this step, or null
     const SrcEntry *src;      // sources inside the updated box, fused
@@ -131,7 +143,7 @@ struct BatchShot {
     long long plane;
     float dt, delta_min;
     float *U[3];
-    const float *K, *E2, *R8;
+    const float *VP, *E2, *R8;
     float *W1[3], *W3[3], *P[3], *W21[2];
     const float4 *layers;
     float *gmax;
@@ -168,6 +180,7 @@ struct BatchArgs {
     const WorkItem *work;
     int nwork;
     int *queue;               // next work item (zeroed by the prepare kernel)
+    int arith;                // Arith of every shot of the batch
 };
 
 // One backward step of the adjoint (qp3d_adjoint.cu): the adjoint state of
@@ -180,7 +193,7 @@ struct AdjParams {
     Coefs k;
     float dt;
     const float *u;                        // u^k
-    const float *K, *E2, *R8;              // (vp dt)^2, 2 eps, 8 (eps - delta)
+    const float *VP, *E2, *R8;             // vp, 2 eps, 8 (eps - delta)
     const float4 *layers;
     const float *T2;                       // threshold m2 of step k
     const float *resid;                    // record residual of step k (hx * hy)
@@ -220,11 +233,11 @@ cudaError_t launch_record(const float *u, float *rec, int nx, int ny, int pml,
 cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0,
                         int y1, int z0, int z1, int ldy, long long plane,
                         cudaStream_t stream);
-// Per-cell parameters (vp dt)^2, 2 eps, 8 (eps - delta), or vp, eps, delta as
+// Per-cell parameters vp, 2 eps, 8 (eps - delta), or vp, eps, delta as
 // IEEE half (round to nearest even), from dense [nz][nx][ny] volumes (the
 // caller's layout, copied to the device in one piece) into the pitched
 // layout, row padding zero.
-cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *K,
+cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *VP,
                                 float *E2, float *R8, int nx, int ny, int nz, int ldy, float dt,
                                 cudaStream_t stream);
 cudaError_t launch_to_half_dense(const float *a, __half *h, int nx, int ny, int nz, int ldy,
@@ -246,7 +259,7 @@ cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threa
 cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,
                                long long max_words, cudaStream_t stream);
 int batch_plane_threads(int tile_x);
-cudaError_t batch_ctas_per_sm(int kind, int threads, size_t smem, int *n);
+cudaError_t batch_ctas_per_sm(int kind, int arith, int threads, size_t smem, int *n);
 cudaError_t configure_gradmax_partial();
 cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid,
                                    size_t smem, cudaStream_t stream, float *partial,

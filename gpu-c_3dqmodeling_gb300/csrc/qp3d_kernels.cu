@@ -42,6 +42,7 @@
 // multiply-adds only, so the oracle reproduces it exactly); the square root
 // is IEEE (sqrt.rn).
 #include "qp3d_internal.h"
+#include "qp3d_exact.h"
 
 #include <math.h>
 
@@ -204,6 +205,18 @@ __device__ __forceinline__ int slot_add(int s, int d)
     return s;
 }
 
+// One second-difference tap in the reference's form, (u[+m] - 2u) + u[-m]
+// (CPU_function.c:393-395), two cells at a time.  Summing c2[m] times these
+// keeps a constant field's Laplacian exactly zero; the form with the centre
+// weight folded into one coefficient, -2 sum(c2[m]) u + sum c2[m](u[+m] +
+// u[-m]), does not (its rounded coefficients leave a term proportional to u),
+// and that systematic term grew to 1.6e-5 relative L2 against the reference
+// arithmetic over a 1000-step shot, against 6.7e-6 with this form.
+__device__ __forceinline__ float2 lap_tap2(float2 a, float2 b, float2 u0)
+{
+    return __fadd2_rn(__ffma2_rn(make_float2(-2.0f, -2.0f), u0, a), b);
+}
+
 template <bool SECOND>
 __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_floats, int t, int rc,
                                             const Coefs &k, float Ux[4], float Uy[4],
@@ -226,24 +239,21 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
         u0[j0] = c0.x;
         u0[j1] = c0.y;
         float2 g = f2(0.0f, 0.0f), l = f2(0.0f, 0.0f);
-        if (SECOND) l = __fmul2_rn(k.ky2, c0);
 #pragma unroll
         for (int m = 0; m < kRadius; ++m) {
             const float2 a = f2(Y[8 + j0 + m + 1], Y[8 + j1 + m + 1]);
             const float2 b = f2(Y[8 + j0 - m - 1], Y[8 + j1 - m - 1]);
             const float2 d = sub2(a, b);
             g = (m == 0) ? __fmul2_rn(k.cy2[0], d) : __ffma2_rn(k.cy2[m], d, g);
-            if (SECOND) l = __ffma2_rn(k.c2y2[m], __fadd2_rn(a, b), l);
+            if (SECOND) l = (m == 0) ? __fmul2_rn(k.c2y2[0], lap_tap2(a, b, c0))
+                                     : __ffma2_rn(k.c2y2[m], lap_tap2(a, b, c0), l);
         }
         Uy[j0] = g.x; Uy[j1] = g.y;
         if (SECOND) { Uyy[j0] = l.x; Uyy[j1] = l.y; }
     }
     // x taps: rows r +- m of the centre plane
+    const float2 uc[2] = {f2(u0[0], u0[1]), f2(u0[2], u0[3])};
     float2 gx[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, lx[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
-    if (SECOND) {
-        lx[0] = __fmul2_rn(k.kx2, f2(u0[0], u0[1]));
-        lx[1] = __fmul2_rn(k.kx2, f2(u0[2], u0[3]));
-    }
 #pragma unroll
     for (int m = 0; m < kRadius; ++m) {
         const float4 a = lds4(pc + rc + (m + 1) * kBoxY);
@@ -253,17 +263,15 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
         for (int h = 0; h < 2; ++h) {
             const float2 d = sub2(a2[h], b2[h]);
             gx[h] = (m == 0) ? __fmul2_rn(k.cx2[0], d) : __ffma2_rn(k.cx2[m], d, gx[h]);
-            if (SECOND) lx[h] = __ffma2_rn(k.c2x2[m], __fadd2_rn(a2[h], b2[h]), lx[h]);
+            if (SECOND) lx[h] = (m == 0) ? __fmul2_rn(k.c2x2[0], lap_tap2(a2[h], b2[h], uc[h]))
+                                         : __ffma2_rn(k.c2x2[m], lap_tap2(a2[h], b2[h], uc[h]),
+                                                      lx[h]);
         }
     }
     Ux[0] = gx[0].x; Ux[1] = gx[0].y; Ux[2] = gx[1].x; Ux[3] = gx[1].y;
     if (SECOND) { Uxx[0] = lx[0].x; Uxx[1] = lx[0].y; Uxx[2] = lx[1].x; Uxx[3] = lx[1].y; }
     // z taps: planes t+5 +- m
     float2 gz[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, lz[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
-    if (SECOND) {
-        lz[0] = __fmul2_rn(k.kz2, f2(u0[0], u0[1]));
-        lz[1] = __fmul2_rn(k.kz2, f2(u0[2], u0[3]));
-    }
 #pragma unroll
     for (int m = 0; m < kRadius; ++m) {
         const float *pp = ring + (size_t)slot_add(sc, m + 1) * slot_floats;
@@ -275,11 +283,136 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
         for (int h = 0; h < 2; ++h) {
             const float2 d = sub2(a2[h], b2[h]);
             gz[h] = (m == 0) ? __fmul2_rn(k.cz2[0], d) : __ffma2_rn(k.cz2[m], d, gz[h]);
-            if (SECOND) lz[h] = __ffma2_rn(k.c2z2[m], __fadd2_rn(a2[h], b2[h]), lz[h]);
+            if (SECOND) lz[h] = (m == 0) ? __fmul2_rn(k.c2z2[0], lap_tap2(a2[h], b2[h], uc[h]))
+                                         : __ffma2_rn(k.c2z2[m], lap_tap2(a2[h], b2[h], uc[h]),
+                                                      lz[h]);
         }
     }
     Uz[0] = gz[0].x; Uz[1] = gz[0].y; Uz[2] = gz[1].x; Uz[3] = gz[1].y;
     if (SECOND) { Uzz[0] = lz[0].x; Uzz[1] = lz[0].y; Uzz[2] = lz[1].x; Uzz[3] = lz[1].y; }
+}
+
+// ---------------------------------------------------------------------------
+// The same derivatives in the reference's arithmetic (CPU_function.c:314-316,
+// 393-395; qp3d_exact.h): per tap c*(u[+m]-u[-m]) / h and
+// c2*((u[+m]-2u) + u[-m]) / h^2, each operation rounded, IEEE division, the
+// taps summed in order from 0.  Products and sums two cells at a time with
+// the packed FP32x2 instructions.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 div2(float2 p, float h)
+{
+    return make_float2(__fdiv_rn(p.x, h), __fdiv_rn(p.y, h));
+}
+
+// one tap of both derivatives for a pair of cells: a = u[+m], b = u[-m]
+__device__ __forceinline__ void tap2(float2 a, float2 b, float2 u0, float2 c, float2 c2, float h,
+                                     float h2, float2 &g, float2 &l)
+{
+    g = __fadd2_rn(g, div2(__fmul2_rn(c, sub2(a, b)), h));
+    l = __fadd2_rn(l, div2(__fmul2_rn(c2, lap_tap2(a, b, u0)), h2));
+}
+
+__device__ __forceinline__ void quad_derivs_ref(const float *ring, size_t slot_floats, int t,
+                                                int rc, const Coefs &k, float Ux[4], float Uy[4],
+                                                float Uz[4], float Uxx[4], float Uyy[4],
+                                                float Uzz[4], float u0[4])
+{
+    const int sc = (t + kRadius) % kRing;
+    const float *pc = ring + (size_t)sc * slot_floats;
+    const float2 zero = make_float2(0.0f, 0.0f);
+    float Y[20];
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+        float4 v = lds4(pc + rc - 8 + 4 * b);
+        Y[4 * b] = v.x; Y[4 * b + 1] = v.y; Y[4 * b + 2] = v.z; Y[4 * b + 3] = v.w;
+    }
+    float2 c0[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int j0 = 2 * h, j1 = 2 * h + 1;
+        c0[h] = f2(Y[8 + j0], Y[8 + j1]);
+        u0[j0] = c0[h].x;
+        u0[j1] = c0[h].y;
+        float2 g = zero, l = zero;
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m)
+            tap2(f2(Y[8 + j0 + m + 1], Y[8 + j1 + m + 1]), f2(Y[8 + j0 - m - 1], Y[8 + j1 - m - 1]),
+                 c0[h], k.rc[m], k.rc2[m], k.rh[1], k.rh2[1], g, l);
+        Uy[j0] = g.x; Uy[j1] = g.y;
+        Uyy[j0] = l.x; Uyy[j1] = l.y;
+    }
+    float2 gx[2] = {zero, zero}, lx[2] = {zero, zero};
+#pragma unroll
+    for (int m = 0; m < kRadius; ++m) {
+        const float4 a = lds4(pc + rc + (m + 1) * kBoxY);
+        const float4 b = lds4(pc + rc - (m + 1) * kBoxY);
+        const float2 a2[2] = {f2(a.x, a.y), f2(a.z, a.w)}, b2[2] = {f2(b.x, b.y), f2(b.z, b.w)};
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            tap2(a2[h], b2[h], c0[h], k.rc[m], k.rc2[m], k.rh[0], k.rh2[0], gx[h], lx[h]);
+    }
+    Ux[0] = gx[0].x; Ux[1] = gx[0].y; Ux[2] = gx[1].x; Ux[3] = gx[1].y;
+    Uxx[0] = lx[0].x; Uxx[1] = lx[0].y; Uxx[2] = lx[1].x; Uxx[3] = lx[1].y;
+    float2 gz[2] = {zero, zero}, lz[2] = {zero, zero};
+#pragma unroll
+    for (int m = 0; m < kRadius; ++m) {
+        const float *pp = ring + (size_t)slot_add(sc, m + 1) * slot_floats;
+        const float *pm = ring + (size_t)slot_add(sc, -m - 1) * slot_floats;
+        const float4 a = lds4(pp + rc);
+        const float4 b = lds4(pm + rc);
+        const float2 a2[2] = {f2(a.x, a.y), f2(a.z, a.w)}, b2[2] = {f2(b.x, b.y), f2(b.z, b.w)};
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            tap2(a2[h], b2[h], c0[h], k.rc[m], k.rc2[m], k.rh[2], k.rh2[2], gz[h], lz[h]);
+    }
+    Uz[0] = gz[0].x; Uz[1] = gz[0].y; Uz[2] = gz[1].x; Uz[3] = gz[1].y;
+    Uzz[0] = lz[0].x; Uzz[1] = lz[0].y; Uzz[2] = lz[1].x; Uzz[3] = lz[1].y;
+}
+
+// First derivatives only, for the gradmax kernels.
+__device__ __forceinline__ void quad_grad_ref(const float *ring, size_t slot_floats, int t, int rc,
+                                              const Coefs &k, float Ux[4], float Uy[4],
+                                              float Uz[4])
+{
+    const int sc = (t + kRadius) % kRing;
+    const float *pc = ring + (size_t)sc * slot_floats;
+    const float2 zero = make_float2(0.0f, 0.0f);
+    float Y[20];
+#pragma unroll
+    for (int b = 0; b < 5; ++b) {
+        float4 v = lds4(pc + rc - 8 + 4 * b);
+        Y[4 * b] = v.x; Y[4 * b + 1] = v.y; Y[4 * b + 2] = v.z; Y[4 * b + 3] = v.w;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int j0 = 2 * h, j1 = 2 * h + 1;
+        float2 g = zero;
+#pragma unroll
+        for (int m = 0; m < kRadius; ++m) {
+            const float2 d = sub2(f2(Y[8 + j0 + m + 1], Y[8 + j1 + m + 1]),
+                                  f2(Y[8 + j0 - m - 1], Y[8 + j1 - m - 1]));
+            g = __fadd2_rn(g, div2(__fmul2_rn(k.rc[m], d), k.rh[1]));
+        }
+        Uy[j0] = g.x; Uy[j1] = g.y;
+    }
+    float2 gx[2] = {zero, zero}, gz[2] = {zero, zero};
+#pragma unroll
+    for (int m = 0; m < kRadius; ++m) {
+        const float4 a = lds4(pc + rc + (m + 1) * kBoxY);
+        const float4 b = lds4(pc + rc - (m + 1) * kBoxY);
+        const float4 za = lds4(ring + (size_t)slot_add(sc, m + 1) * slot_floats + rc);
+        const float4 zb = lds4(ring + (size_t)slot_add(sc, -m - 1) * slot_floats + rc);
+        const float2 a2[2] = {f2(a.x, a.y), f2(a.z, a.w)}, b2[2] = {f2(b.x, b.y), f2(b.z, b.w)};
+        const float2 za2[2] = {f2(za.x, za.y), f2(za.z, za.w)},
+                     zb2[2] = {f2(zb.x, zb.y), f2(zb.z, zb.w)};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            gx[h] = __fadd2_rn(gx[h], div2(__fmul2_rn(k.rc[m], sub2(a2[h], b2[h])), k.rh[0]));
+            gz[h] = __fadd2_rn(gz[h], div2(__fmul2_rn(k.rc[m], sub2(za2[h], zb2[h])), k.rh[2]));
+        }
+    }
+    Ux[0] = gx[0].x; Ux[1] = gx[0].y; Ux[2] = gx[1].x; Ux[3] = gx[1].y;
+    Uz[0] = gz[0].x; Uz[1] = gz[0].y; Uz[2] = gz[1].x; Uz[3] = gz[1].y;
 }
 
 // ---------------------------------------------------------------------------
@@ -405,7 +538,7 @@ __device__ void pipe_inval(const Pipe &P)
 // planes in registers (loop unrolled by 11 so the queue never moves), which
 // leaves 16 shared-memory vector loads per quad and plane instead of 25.
 // ---------------------------------------------------------------------------
-template <bool QUEUE>
+template <bool QUEUE, int AR>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_gradmax_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
@@ -513,7 +646,11 @@ __global__ void __launch_bounds__(kThreads, 2)
             if (!ok) break;
             if (row_ok) {
                 float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
-                quad_derivs<false>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+                if (AR == kArithRef)
+                    quad_grad_ref(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz);
+                else
+                    quad_derivs<false>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy,
+                                       Uzz, u0);
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
                     if (cell_ok[j])
@@ -538,7 +675,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 // are invalidated at the end so that it can take another tile; the return
 // value (false: a wait timed out) is then the same in every thread.
 // ---------------------------------------------------------------------------
-template <bool REUSE>
+template <bool REUSE, int AR = kArithFast>
 __device__ __forceinline__ bool gradmax_tile(const CUtensorMap *tm, const PlaneParams &p,
                                              const Coefs &k, int tile_x, int y0, int x0, int z0,
                                              int z1, unsigned char *smem)
@@ -574,7 +711,10 @@ __device__ __forceinline__ bool gradmax_tile(const CUtensorMap *tm, const PlaneP
         if (!ok) break;
         if (row_ok) {
             float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
-            quad_derivs<false>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+            if (AR == kArithRef)
+                quad_grad_ref(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz);
+            else
+                quad_derivs<false>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 if (cell_ok[j])
@@ -603,6 +743,7 @@ __device__ __forceinline__ bool gradmax_tile(const CUtensorMap *tm, const PlaneP
 // partial[linear CTA index] (every CTA writes its slot, also when it has no
 // cell), for callers that supply the partial array themselves.
 // ---------------------------------------------------------------------------
+template <int AR>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_gradmax_partial_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p,
                                 float *partial)
@@ -648,7 +789,11 @@ __global__ void __launch_bounds__(kThreads, 2)
         if (!ok) break;
         if (row_ok) {
             float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
-            quad_derivs<false>(P.ring, P.slot_floats, t, rc, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+            if (AR == kArithRef)
+                quad_grad_ref(P.ring, P.slot_floats, t, rc, p.k, Ux, Uy, Uz);
+            else
+                quad_derivs<false>(P.ring, P.slot_floats, t, rc, p.k, Ux, Uy, Uz, Uxx, Uyy, Uzz,
+                                   u0);
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 if (cell_ok[j])
@@ -852,13 +997,10 @@ __device__ __forceinline__ float2 aniso_s2(float2 h2, float2 m2, float2 v2, floa
     return __ffma2_rn(half, make_float2(__fsqrt_rn(t.x), __fsqrt_rn(t.y)), half);
 }
 
-// One tile column [z0, z1) of the step.  The grid kernel below runs one per
-// CTA; the batched kernel runs many per CTA (REUSE: barriers invalidated at
-// the end, return value uniform over the CTA; false = a wait timed out).
 // Per-cell parameters of a quad from half-precision vp, eps, delta, with the
-// operations of qp3d_params_dense_kernel: (vp dt)^2, 2 eps, 8 (eps - delta).
-__device__ __forceinline__ void quad_params_half(const PlaneParams &p, uint2 hv, uint2 he,
-                                                 uint2 hd, float4 &K, float4 &E2, float4 &R8)
+// operations of qp3d_params_dense_kernel: vp, 2 eps, 8 (eps - delta).
+__device__ __forceinline__ void quad_params_half(uint2 hv, uint2 he, uint2 hd, float4 &V,
+                                                 float4 &E2, float4 &R8)
 {
     const float2 v0 = __half22float2(*reinterpret_cast<const __half2 *>(&hv.x));
     const float2 v1 = __half22float2(*reinterpret_cast<const __half2 *>(&hv.y));
@@ -866,22 +1008,38 @@ __device__ __forceinline__ void quad_params_half(const PlaneParams &p, uint2 hv,
     const float2 e1 = __half22float2(*reinterpret_cast<const __half2 *>(&he.y));
     const float2 d0 = __half22float2(*reinterpret_cast<const __half2 *>(&hd.x));
     const float2 d1 = __half22float2(*reinterpret_cast<const __half2 *>(&hd.y));
-    const float vp[4] = {v0.x, v0.y, v1.x, v1.y}, ep[4] = {e0.x, e0.y, e1.x, e1.y},
-                de[4] = {d0.x, d0.y, d1.x, d1.y};
-    float k[4], e[4], r[4];
+    const float ep[4] = {e0.x, e0.y, e1.x, e1.y}, de[4] = {d0.x, d0.y, d1.x, d1.y};
+    float e[4], r[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const float vdt = __fmul_rn(vp[j], p.dt);
-        k[j] = __fmul_rn(vdt, vdt);
         e[j] = __fmul_rn(2.0f, ep[j]);
         r[j] = __fmul_rn(8.0f, __fsub_rn(ep[j], de[j]));
     }
-    K = make_float4(k[0], k[1], k[2], k[3]);
+    V = make_float4(v0.x, v0.y, v1.x, v1.y);
     E2 = make_float4(e[0], e[1], e[2], e[3]);
     R8 = make_float4(r[0], r[1], r[2], r[3]);
 }
 
-template <bool SPEC, bool REUSE, bool HALF = false>
+// (vp dt)^2 of the fast arithmetic
+__device__ __forceinline__ float k_of_vp(float vp, float dt)
+{
+    const float vdt = __fmul_rn(vp, dt);
+    return __fmul_rn(vdt, vdt);
+}
+
+// The fast arithmetic's layer coefficients from the stored (a1h, a1l, d*dt, dd):
+// a1 = RN(a1h + a1l) = a1h, a2 = 2*d*dt - 1, a3 = 1 - d*dt.
+__device__ __forceinline__ float4 fast_layer(float4 t)
+{
+    return make_float4(t.x, __fmaf_rn(2.0f, t.z, -1.0f), __fsub_rn(1.0f, t.z), t.w);
+}
+
+// One tile column [z0, z1) of the step.  The grid kernel below runs one per
+// CTA; the batched kernel runs many per CTA (REUSE: barriers invalidated at
+// the end, return value uniform over the CTA; false = a wait timed out).
+// AR: kArithRef (the reference CPU operators' roundings, qp3d_exact.h) or
+// kArithFast (folded coefficients, fused multiply-adds, one reciprocal in S).
+template <bool SPEC, bool REUSE, bool HALF = false, int AR = kArithFast>
 __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlaneParams &p,
                                           const Coefs &k, int tile_x, int y0, int x0, int z0,
                                           int z1, bool win_writer, unsigned char *smem)
@@ -897,7 +1055,6 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
     const int nzc = z1 - z0;
     Pipe P;
     pipe_setup(P, smem, tile_x, p.pml, y0, x0, z0, nzc);
-
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml;
     int next_issue = 0;
     if (tid == 0) {
@@ -952,6 +1109,11 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
     const bool xy_face = row_ok && (fx >= 0 || any_fy);
     const int hy = ny - 2 * pml;
     const float dt = p.dt;
+    const float dt2 = __fmul_rn(dt, dt);
+    // the reference adds source * wavelet to every cell (CPU_function.c:326-338):
+    // a cell without a source gets +-0, which turns a -0 into +0 when the
+    // product is +0
+    const float zw = __fmul_rn(0.0f, p.wavelet);
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
 
     float mx = 0.0f;
@@ -963,7 +1125,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         const int fz = z < pml ? 4 : (z >= nz - pml ? 5 : -1);
         const int liz = z < pml ? pml - z : z - nz + pml;
         const bool pml_quad = xy_face || (row_ok && fz >= 0);
-        float4 u1v = zero4, Kv = zero4, Ev = zero4, Rv = zero4;
+        float4 u1v = zero4, Vv = zero4, Ev = zero4, Rv = zero4;
         uint2 hv = make_uint2(0u, 0u), he = hv, hd = hv;
         if (row_ok) {
             u1v = ldg4(p.u_prev + base);
@@ -972,7 +1134,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                 he = __ldg(reinterpret_cast<const uint2 *>(p.h_eps + base));
                 hd = __ldg(reinterpret_cast<const uint2 *>(p.h_del + base));
             } else {
-                Kv = ldg4(p.prm_k + base);
+                Vv = ldg4(p.prm_v + base);
                 Ev = ldg4(p.prm_e + base);
                 Rv = ldg4(p.prm_r + base);
             }
@@ -993,24 +1155,42 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         ok = __all_sync(0xffffffffu, ok);   // warps stay converged for the collectives below
         if (!ok) break;
         float Ux[4], Uy[4], Uz[4], Uxx[4], Uyy[4], Uzz[4], u0[4];
-        quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
-        if (HALF) quad_params_half(p, hv, he, hd, Kv, Ev, Rv);
-        // scalar operator, GPU_kernel.cu:93-111
+        if (AR == kArithRef)
+            quad_derivs_ref(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        else
+            quad_derivs<true>(P.ring, P.slot_floats, t, rc, k, Ux, Uy, Uz, Uxx, Uyy, Uzz, u0);
+        if (HALF) quad_params_half(hv, he, hd, Vv, Ev, Rv);
+        // scalar operator, GPU_kernel.cu:93-111 / CPU_function.c:339-370
         float h2[4], m2[4];
         bool above[4], amb[4];
         bool any_above = false;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            h2[j] = fmaf(Uy[j], Uy[j], __fmul_rn(Ux[j], Ux[j]));
-            m2[j] = fmaf(Uz[j], Uz[j], h2[j]);
+            if (AR == kArithRef) {
+                m2[j] = xr::grad_m2(Ux[j], Uy[j], Uz[j]);
+                h2[j] = 0.0f;
+            } else {
+                h2[j] = fmaf(Uy[j], Uy[j], __fmul_rn(Ux[j], Ux[j]));
+                m2[j] = fmaf(Uz[j], Uz[j], h2[j]);
+            }
             if (SPEC && cell_ok[j])
                 mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
             above[j] = m2[j] > T2lo;
             amb[j] = SPEC && cell_ok[j] && above[j] && !(m2[j] > T2hi);
             any_above = any_above || (row_ok && above[j]);
         }
-        float KS[4], e2[4];
-        if (__any_sync(0xffffffffu, any_above)) {
+        float S[4], e1[4];   // S; 1 + 2 eps
+        float KS[4];         // fast arithmetic: (vp dt)^2 S
+#pragma unroll
+        for (int j = 0; j < 4; ++j) e1[j] = __fadd_rn(1.0f, f4(Ev, j));
+        if (AR == kArithRef) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                S[j] = 1.0f;
+                if (cell_ok[j] && above[j])
+                    S[j] = xr::scalar_s(Ux[j], Uy[j], Uz[j], m2[j], f4(Ev, j), f4(Rv, j));
+            }
+        } else if (__any_sync(0xffffffffu, any_above)) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) {   // cells (0,1) and (2,3) as pairs
                 const int j0 = 2 * h, j1 = 2 * h + 1;
@@ -1019,22 +1199,27 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                                                      make_float2(Uz[j0], Uz[j1])),
                                           make_float2(f4(Ev, j0), f4(Ev, j1)),
                                           make_float2(f4(Rv, j0), f4(Rv, j1)));
-                KS[j0] = __fmul_rn(f4(Kv, j0), above[j0] ? s.x : 1.0f);
-                KS[j1] = __fmul_rn(f4(Kv, j1), above[j1] ? s.y : 1.0f);
+                KS[j0] = __fmul_rn(k_of_vp(f4(Vv, j0), dt), above[j0] ? s.x : 1.0f);
+                KS[j1] = __fmul_rn(k_of_vp(f4(Vv, j1), dt), above[j1] ? s.y : 1.0f);
             }
         } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) KS[j] = __fmul_rn(f4(Kv, j), 1.0f);
+            for (int j = 0; j < 4; ++j) KS[j] = __fmul_rn(k_of_vp(f4(Vv, j), dt), 1.0f);
         }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) e2[j] = __fadd_rn(1.0f, f4(Ev, j));
         float out[4], alt[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float Lp = fmaf(e2[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
-            const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
-            out[j] = fmaf(KS[j], Lp, lin);
-            alt[j] = fmaf(__fmul_rn(f4(Kv, j), 1.0f), Lp, lin);   // S = 1, for deferred cells
+            if (AR == kArithRef) {
+                out[j] = xr::interior_update(u0[j], f4(u1v, j), Uxx[j], Uyy[j], Uzz[j], e1[j],
+                                             S[j], f4(Vv, j), dt2);
+                alt[j] = xr::interior_update(u0[j], f4(u1v, j), Uxx[j], Uyy[j], Uzz[j], e1[j],
+                                             1.0f, f4(Vv, j), dt2);   // S = 1, deferred cells
+            } else {
+                const float Lp = fmaf(e1[j], __fadd_rn(Uxx[j], Uyy[j]), Uzz[j]);
+                const float lin = fmaf(2.0f, u0[j], -f4(u1v, j));
+                out[j] = fmaf(KS[j], Lp, lin);
+                alt[j] = fmaf(__fmul_rn(k_of_vp(f4(Vv, j), dt), 1.0f), Lp, lin);
+            }
         }
         if (__any_sync(0xffffffffu, pml_quad)) {
             float n13[4], n21[4], n33[4], n3[4];
@@ -1043,33 +1228,68 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                 int f, li;
                 cell_face(fx, lix, fy[j], liy[j], fz, liz, f, li);
                 const bool is_pml = pml_quad && cell_ok[j] && f >= 0;
-                const float4 lc = tab[is_pml ? (f >> 1) * pml + li : 0];
-                float v;
-                if (SPEC) {
-                    // also the S = 1 update of the cell and its split-field
-                    // outputs, kept for a deferred cell's fix-up (computing
-                    // both for every cell keeps the loop free of branches)
-                    float v1;
-                    float4 a1x;
-                    v = pml_cell2(f < 0 ? 0 : f, lc, KS[j], __fmul_rn(f4(Kv, j), 1.0f), e2[j],
-                                  Ux[j], Uy[j], Uz[j], Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j),
-                                  f4(w12, j), f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
-                                  f4(p2, j), n13[j], n21[j], n33[j], n3[j], v1, a1x);
-                    if (is_pml && amb[j]) {
-                        alt[j] = v1;
-                        p.apml[base + j] = a1x;
+                const float4 lt = tab[is_pml ? (f >> 1) * pml + li : 0];
+                if (AR == kArithRef) {
+                    n13[j] = n33[j] = n3[j] = 0.0f;
+                    n21[j] = f4(w21, j);
+                    if (is_pml) {
+                        const bool isx = f < 2, isz = f >= 4;
+                        xr::PmlLayer Lr;
+                        Lr.a1h = lt.x; Lr.a1l = lt.y;
+                        Lr.a2 = __fmaf_rn(2.0f, lt.z, -1.0f);
+                        Lr.a3 = __fsub_rn(1.0f, lt.z);
+                        Lr.dd = lt.w;
+                        const float Unn = isx ? Uxx[j] : (isz ? Uzz[j] : Uyy[j]);
+                        const float Un = isx ? Ux[j] : (isz ? Uz[j] : Uy[j]);
+                        const float tang = isz ? __fadd_rn(Uxx[j], Uyy[j])
+                                               : __fadd_rn(Uzz[j], __fmul_rn(e1[j], isx ? Uyy[j] : Uxx[j]));
+                        const float vdt = __fmul_rn(f4(Vv, j), dt);
+                        const xr::PmlOut o = xr::pml_update(isz, (f & 1) != 0, S[j], e1[j], vdt,
+                                                            Unn, Un, tang, dt, Lr, f4(w11, j),
+                                                            f4(w12, j), f4(w21, j), f4(w31, j),
+                                                            f4(w32, j), f4(p1, j), f4(p2, j));
+                        out[j] = o.u3;
+                        n13[j] = o.w13; n21[j] = o.w21; n33[j] = o.w33; n3[j] = o.p3;
+                        if (SPEC && amb[j]) {   // the S = 1 update, kept for the fix-up
+                            const xr::PmlOut o1 = xr::pml_update(isz, (f & 1) != 0, 1.0f, e1[j],
+                                                                 vdt, Unn, Un, tang, dt, Lr,
+                                                                 f4(w11, j), f4(w12, j),
+                                                                 f4(w21, j), f4(w31, j),
+                                                                 f4(w32, j), f4(p1, j), f4(p2, j));
+                            alt[j] = o1.u3;
+                            p.apml[base + j] = make_float4(o1.w13, o1.w21, o1.w33, o1.p3);
+                        }
                     }
                 } else {
-                    v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e2[j], Ux[j], Uy[j], Uz[j], Uxx[j],
-                                 Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j), f4(w21, j),
-                                 f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j), n13[j], n21[j],
-                                 n33[j], n3[j]);
+                    const float4 lc = fast_layer(lt);
+                    float v;
+                    if (SPEC) {
+                        // also the S = 1 update of the cell and its split-field
+                        // outputs, kept for a deferred cell's fix-up (computing
+                        // both for every cell keeps the loop free of branches)
+                        float v1;
+                        float4 a1x;
+                        v = pml_cell2(f < 0 ? 0 : f, lc, KS[j],
+                                      __fmul_rn(k_of_vp(f4(Vv, j), dt), 1.0f), e1[j], Ux[j],
+                                      Uy[j], Uz[j], Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j),
+                                      f4(w12, j), f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
+                                      f4(p2, j), n13[j], n21[j], n33[j], n3[j], v1, a1x);
+                        if (is_pml && amb[j]) {
+                            alt[j] = v1;
+                            p.apml[base + j] = a1x;
+                        }
+                    } else {
+                        v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e1[j], Ux[j], Uy[j], Uz[j],
+                                     Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
+                                     f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
+                                     n13[j], n21[j], n33[j], n3[j]);
+                    }
+                    out[j] = is_pml ? v : out[j];
+                    n13[j] = is_pml ? n13[j] : 0.0f;
+                    n33[j] = is_pml ? n33[j] : 0.0f;
+                    n3[j] = is_pml ? n3[j] : 0.0f;
+                    n21[j] = is_pml ? n21[j] : f4(w21, j);
                 }
-                out[j] = is_pml ? v : out[j];
-                n13[j] = is_pml ? n13[j] : 0.0f;
-                n33[j] = is_pml ? n33[j] : 0.0f;
-                n3[j] = is_pml ? n3[j] : 0.0f;
-                n21[j] = is_pml ? n21[j] : f4(w21, j);
             }
             if (pml_quad) {
                 *reinterpret_cast<float4 *>(p.w1n + base) = make_float4(n13[0], n13[1], n13[2], n13[3]);
@@ -1078,7 +1298,8 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                 *reinterpret_cast<float4 *>(p.w21n + base) = make_float4(n21[0], n21[1], n21[2], n21[3]);
             }
         }
-        // source injection (GPU_kernel.cu:727): u3 += source * wavelet
+        // source injection (GPU_kernel.cu:727, CPU_function.c:334): u3 += source * wavelet
+        bool has_src[4] = {false, false, false, false};
         for (int e = 0; e < ncsrc; ++e) {
             const SrcEntry s = csrc[e];
             if (s.z == z && s.x == x) {
@@ -1089,8 +1310,17 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                     if (jj == js) {
                         out[jj] = __fadd_rn(out[jj], add);
                         alt[jj] = __fadd_rn(alt[jj], add);
+                        has_src[jj] = true;
                     }
             }
+        }
+        if (AR == kArithRef) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (!has_src[j]) {
+                    out[j] = __fadd_rn(out[j], zw);
+                    alt[j] = __fadd_rn(alt[j], zw);
+                }
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) out[j] = cell_ok[j] ? out[j] : u0[j];   // never updated
@@ -1142,7 +1372,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
     return ok;
 }
 
-template <bool SPEC, bool HALF>
+template <bool SPEC, bool HALF, int AR>
 __global__ void __launch_bounds__(kThreads, 2)
     qp3d_step_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
@@ -1152,8 +1382,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int z0 = kRadius + blockIdx.z * p.chunk_z;
     const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
     if (z0 >= z1) return;
-    step_tile<SPEC, false, HALF>(&tm_u, p, p.k, p.tile_x, y0, x0, z0, z1,
-                                 blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
+    step_tile<SPEC, false, HALF, AR>(&tm_u, p, p.k, p.tile_x, y0, x0, z0, z1,
+                                     blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
 }
 
 // Resolution of a speculative step, one thread: whether the true max fell in
@@ -1422,7 +1652,7 @@ __global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, Pl
             const int a = (3 - k % 3) % 3, bb = (a + 1) % 3, c = (a + 2) % 3;
             p.ucur = a;
             p.u_cur = b.U[a]; p.u_prev = b.U[bb]; p.u_out = b.U[c];
-            p.prm_k = b.K; p.prm_e = b.E2; p.prm_r = b.R8;
+            p.prm_v = b.VP; p.prm_e = b.E2; p.prm_r = b.R8;
             const int lo = k % 3, lc = (k + 1) % 3, ln = (k + 2) % 3;
             p.w1o = b.W1[lo]; p.w1c = b.W1[lc]; p.w1n = b.W1[ln];
             p.w3o = b.W3[lo]; p.w3c = b.W3[lc]; p.w3n = b.W3[ln];
@@ -1469,7 +1699,7 @@ size_t batch_smem_bytes(int tile_x, int pml, int nsrc)
 
 // KIND 0: gradmax, 1: exact step (skipped for shots whose gate is 0),
 // 2: speculative step.
-template <int KIND>
+template <int KIND, int AR>
 __global__ void __launch_bounds__(kThreads, 2) qp3d_batch_plane_kernel(const __grid_constant__ BatchArgs b)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1512,11 +1742,11 @@ __global__ void __launch_bounds__(kThreads, 2) qp3d_batch_plane_kernel(const __g
         tm += p.ucur;
         bool ok;
         if (KIND == 0) {
-            ok = gradmax_tile<true>(tm, p, b.k, w.tile_x, w.y0, w.x0, w.z0, w.z1, body);
+            ok = gradmax_tile<true, AR>(tm, p, b.k, w.tile_x, w.y0, w.x0, w.z0, w.z1, body);
         } else {
             const bool first = w.y0 == 0 && w.x0 == kRadius && w.z0 == kRadius;
-            ok = step_tile<KIND == 2, true>(tm, p, b.k, w.tile_x, w.y0, w.x0, w.z0, w.z1, first,
-                                            body);
+            ok = step_tile<KIND == 2, true, false, AR>(tm, p, b.k, w.tile_x, w.y0, w.x0, w.z0,
+                                                       w.z1, first, body);
         }
         if (!ok) return;
     }
@@ -1666,8 +1896,10 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
             }
         }
         // frozen scalar operator and its eps / delta derivatives
-        const float4 Kv = ldg4_or0(a.K, i, true), Ev = ldg4_or0(a.E2, i, true),
+        const float4 Vv = ldg4_or0(a.VP, i, true), Ev = ldg4_or0(a.E2, i, true),
                      Rv = ldg4_or0(a.R8, i, true);
+        const float4 Kv = make_float4(k_of_vp(Vv.x, a.dt), k_of_vp(Vv.y, a.dt),
+                                      k_of_vp(Vv.z, a.dt), k_of_vp(Vv.w, a.dt));
         const float T2 = *a.T2;
         float KS[4], e2[4], S[4], dSe[4], dSd[4];
 #pragma unroll
@@ -1891,33 +2123,34 @@ __global__ void qp3d_from_bf16_kernel(const __nv_bfloat16 *h, float *a, long lon
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+template <typename F>
+static cudaError_t set_smem(F *fn, int bytes)
+{
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 cudaError_t configure_kernels()
 {
     const int bytes = 200 * 1024;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<0>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+    if ((e = set_smem(qp3d_batch_plane_kernel<0, kArithFast>, bytes)) ||
+        (e = set_smem(qp3d_batch_plane_kernel<1, kArithFast>, bytes)) ||
+        (e = set_smem(qp3d_batch_plane_kernel<2, kArithFast>, bytes)) ||
+        (e = set_smem(qp3d_batch_plane_kernel<0, kArithRef>, bytes)) ||
+        (e = set_smem(qp3d_batch_plane_kernel<1, kArithRef>, bytes)) ||
+        (e = set_smem(qp3d_batch_plane_kernel<2, kArithRef>, bytes)))
         return e;
-    if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<1>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
+#define QP3D_STEP_SMEM(AR)                                                                   \
+    if ((e = set_smem(qp3d_step_kernel<true, false, AR>, bytes)) ||                         \
+        (e = set_smem(qp3d_step_kernel<false, false, AR>, bytes)) ||                        \
+        (e = set_smem(qp3d_step_kernel<true, true, AR>, bytes)) ||                          \
+        (e = set_smem(qp3d_step_kernel<false, true, AR>, bytes)) ||                         \
+        (e = set_smem(qp3d_gradmax_kernel<false, AR>, bytes)))                              \
         return e;
-    if ((e = cudaFuncSetAttribute(qp3d_batch_plane_kernel<2>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    if ((e = cudaFuncSetAttribute(qp3d_step_kernel<true, false>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
-        (e = cudaFuncSetAttribute(qp3d_step_kernel<false, false>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
-        (e = cudaFuncSetAttribute(qp3d_step_kernel<true, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) ||
-        (e = cudaFuncSetAttribute(qp3d_step_kernel<false, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    if ((e = cudaFuncSetAttribute(qp3d_gradmax_kernel<true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)))
-        return e;
-    return cudaFuncSetAttribute(qp3d_gradmax_kernel<false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    QP3D_STEP_SMEM(kArithFast)
+    QP3D_STEP_SMEM(kArithRef)
+#undef QP3D_STEP_SMEM
+    return set_smem(qp3d_gradmax_kernel<true, kArithFast>, bytes);
 }
 
 // whole warps: rows past tile_x are idle, so every warp collective sees 32 lanes
@@ -1926,38 +2159,54 @@ static inline int plane_threads(int tile_x) { return (kQuadsY * tile_x + 31) & ~
 cudaError_t launch_gradmax(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
                            cudaStream_t stream, int variant)
 {
-    if (variant == 0)
-        qp3d_gradmax_kernel<false><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+    const int t = plane_threads(p.tile_x);
+    if (p.arith == kArithRef)
+        qp3d_gradmax_kernel<false, kArithRef><<<grid, t, smem, stream>>>(tm_u, p);
+    else if (variant == 0)
+        qp3d_gradmax_kernel<false, kArithFast><<<grid, t, smem, stream>>>(tm_u, p);
     else
-        qp3d_gradmax_kernel<true><<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p);
+        qp3d_gradmax_kernel<true, kArithFast><<<grid, t, smem, stream>>>(tm_u, p);
     return cudaGetLastError();
+}
+
+template <int AR>
+static void launch_step_t(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, int t,
+                          size_t smem, cudaStream_t stream)
+{
+    if (p.half_params) {
+        if (p.spec) qp3d_step_kernel<true, true, AR><<<grid, t, smem, stream>>>(tm_u, p);
+        else qp3d_step_kernel<false, true, AR><<<grid, t, smem, stream>>>(tm_u, p);
+    } else {
+        if (p.spec) qp3d_step_kernel<true, false, AR><<<grid, t, smem, stream>>>(tm_u, p);
+        else qp3d_step_kernel<false, false, AR><<<grid, t, smem, stream>>>(tm_u, p);
+    }
 }
 
 cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid, size_t smem,
                         cudaStream_t stream)
 {
     const int t = plane_threads(p.tile_x);
-    if (p.half_params) {
-        if (p.spec) qp3d_step_kernel<true, true><<<grid, t, smem, stream>>>(tm_u, p);
-        else qp3d_step_kernel<false, true><<<grid, t, smem, stream>>>(tm_u, p);
-    } else {
-        if (p.spec) qp3d_step_kernel<true, false><<<grid, t, smem, stream>>>(tm_u, p);
-        else qp3d_step_kernel<false, false><<<grid, t, smem, stream>>>(tm_u, p);
-    }
+    if (p.arith == kArithRef) launch_step_t<kArithRef>(tm_u, p, grid, t, smem, stream);
+    else launch_step_t<kArithFast>(tm_u, p, grid, t, smem, stream);
     return cudaGetLastError();
 }
 
 cudaError_t configure_gradmax_partial()
 {
-    return cudaFuncSetAttribute(qp3d_gradmax_partial_kernel,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e;
+    if ((e = set_smem(qp3d_gradmax_partial_kernel<kArithFast>, 200 * 1024))) return e;
+    return set_smem(qp3d_gradmax_partial_kernel<kArithRef>, 200 * 1024);
 }
 
 cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p, dim3 grid,
                                    size_t smem, cudaStream_t stream, float *partial,
                                    unsigned nblocks, float *out)
 {
-    qp3d_gradmax_partial_kernel<<<grid, plane_threads(p.tile_x), smem, stream>>>(tm_u, p, partial);
+    const int t = plane_threads(p.tile_x);
+    if (p.arith == kArithRef)
+        qp3d_gradmax_partial_kernel<kArithRef><<<grid, t, smem, stream>>>(tm_u, p, partial);
+    else
+        qp3d_gradmax_partial_kernel<kArithFast><<<grid, t, smem, stream>>>(tm_u, p, partial);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     qp3d_reduce_max_kernel<<<1, 1024, 0, stream>>>(partial, nblocks, p.err, out);
@@ -1986,24 +2235,29 @@ cudaError_t launch_batch_prepare(const BatchShot *shots, int nshots, PlaneParams
     return cudaGetLastError();
 }
 
-cudaError_t batch_ctas_per_sm(int kind, int threads, size_t smem, int *n)
+static const void *batch_plane_fn(int kind, int arith)
 {
-    const void *f = kind == 0 ? (const void *)qp3d_batch_plane_kernel<0>
-                  : kind == 1 ? (const void *)qp3d_batch_plane_kernel<1>
-                              : (const void *)qp3d_batch_plane_kernel<2>;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, f, threads, smem);
+    if (arith == kArithRef)
+        return kind == 0 ? (const void *)qp3d_batch_plane_kernel<0, kArithRef>
+             : kind == 1 ? (const void *)qp3d_batch_plane_kernel<1, kArithRef>
+                         : (const void *)qp3d_batch_plane_kernel<2, kArithRef>;
+    return kind == 0 ? (const void *)qp3d_batch_plane_kernel<0, kArithFast>
+         : kind == 1 ? (const void *)qp3d_batch_plane_kernel<1, kArithFast>
+                     : (const void *)qp3d_batch_plane_kernel<2, kArithFast>;
+}
+
+cudaError_t batch_ctas_per_sm(int kind, int arith, int threads, size_t smem, int *n)
+{
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, batch_plane_fn(kind, arith), threads,
+                                                         smem);
 }
 
 cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threads, size_t smem,
                                cudaStream_t stream)
 {
-    if (kind == 0)
-        qp3d_batch_plane_kernel<0><<<grid, threads, smem, stream>>>(b);
-    else if (kind == 1)
-        qp3d_batch_plane_kernel<1><<<grid, threads, smem, stream>>>(b);
-    else
-        qp3d_batch_plane_kernel<2><<<grid, threads, smem, stream>>>(b);
-    return cudaGetLastError();
+    void *args[] = {const_cast<BatchArgs *>(&b)};
+    return cudaLaunchKernel(batch_plane_fn(kind, b.arith), dim3(grid), dim3(threads), args, smem,
+                            stream);
 }
 
 cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,

@@ -152,6 +152,7 @@ extern "C" int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, in
     p.chunk_z = chunk_z;
     p.plane = (long long)nx * ldy;
     derive_coefs(c, c, dx, dy, dz, &p.k);   // first-derivative weights only
+    p.arith = kArithFast;   // the library's default arithmetic
     p.err = ds.err;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the error word must start at zero; the partial slots are all written

@@ -418,14 +418,12 @@ static void ref32_update(st32 *s, const oracle_args *a)
 typedef struct {
     float cx[R], cy[R], cz[R];        /* c[30+m]/h */
     float c2x[R], c2y[R], c2z[R];     /* c2[30+m]/(h*h) */
-    float kx, ky, kz;                 /* -2*sum(c2?) : centre tap */
 } mirror_coef;
 
 static void mirror_coef_init(mirror_coef *k, const float *c, const float *c2,
                              float dx, float dy, float dz)
 {
     float dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     for (int m = 0; m < R; m++) {
         k->cx[m] = c[31 + m] / dx;
         k->cy[m] = c[31 + m] / dy;
@@ -433,26 +431,20 @@ static void mirror_coef_init(mirror_coef *k, const float *c, const float *c2,
         k->c2x[m] = c2[31 + m] / dx2;
         k->c2y[m] = c2[31 + m] / dy2;
         k->c2z[m] = c2[31 + m] / dz2;
-        sx = sx + k->c2x[m];
-        sy = sy + k->c2y[m];
-        sz = sz + k->c2z[m];
     }
-    k->kx = -(2.0f * sx);
-    k->ky = -(2.0f * sy);
-    k->kz = -(2.0f * sz);
 }
 
 /* Derivatives of u at cell i along one axis with stride st. */
 static inline void mirror_axis(const float *u, size_t i, size_t st,
-                               const float *cc, const float *c2c, float kc,
-                               float *U1, float *U2)
+                               const float *cc, const float *c2c, float *U1, float *U2)
 {
-    float g = 0.0f, l = kc * u[i];
+    float g = 0.0f, l = 0.0f;
     for (int m = 0; m < R; m++) {
         float p = u[i + (m + 1) * st], q = u[i - (m + 1) * st];
-        float dmm = p - q, smm = p + q;
+        /* second difference in the reference's form (u[+m] - 2u) + u[-m] */
+        float dmm = p - q, smm = fmaf(-2.0f, u[i], p) + q;
         g = (m == 0) ? cc[0] * dmm : fmaf(cc[m], dmm, g);
-        l = fmaf(c2c[m], smm, l);
+        l = (m == 0) ? c2c[0] * smm : fmaf(c2c[m], smm, l);
     }
     *U1 = g;
     *U2 = l;
@@ -472,9 +464,9 @@ static float mirror_gradmax(st32 *s, const mirror_coef *k)
                 for (int y = R; y < ny - R; y++) {
                     size_t i = IX(z, x, y);
                     float Ux, Uy, Uz, t;
-                    mirror_axis(u, i, (size_t)ny, k->cx, k->c2x, k->kx, &Ux, &t);
-                    mirror_axis(u, i, 1, k->cy, k->c2y, k->ky, &Uy, &t);
-                    mirror_axis(u, i, (size_t)nx * ny, k->cz, k->c2z, k->kz, &Uz, &t);
+                    mirror_axis(u, i, (size_t)ny, k->cx, k->c2x, &Ux, &t);
+                    mirror_axis(u, i, 1, k->cy, k->c2y, &Uy, &t);
+                    mirror_axis(u, i, (size_t)nx * ny, k->cz, k->c2z, &Uz, &t);
                     lm = fmaxf(lm, fmaxf(fabsf(Ux), fmaxf(fabsf(Uy), fabsf(Uz))));
                 }
 #pragma omp critical
@@ -527,9 +519,9 @@ static void mirror_update(st32 *s, const oracle_args *a, const mirror_coef *k,
             for (int y = R; y < ny - R; y++) {
                 size_t i = IX(z, x, y);
                 float Ux, Uy, Uz, Uxx, Uyy, Uzz;
-                mirror_axis(u2, i, (size_t)ny, k->cx, k->c2x, k->kx, &Ux, &Uxx);
-                mirror_axis(u2, i, 1, k->cy, k->c2y, k->ky, &Uy, &Uyy);
-                mirror_axis(u2, i, (size_t)nx * ny, k->cz, k->c2z, k->kz, &Uz, &Uzz);
+                mirror_axis(u2, i, (size_t)ny, k->cx, k->c2x, &Ux, &Uxx);
+                mirror_axis(u2, i, 1, k->cy, k->c2y, &Uy, &Uyy);
+                mirror_axis(u2, i, (size_t)nx * ny, k->cz, k->c2z, &Uz, &Uzz);
                 /* per-cell parameters as stored on the device */
                 float vdt = a->vp[i] * dt;
                 float K = vdt * vdt;

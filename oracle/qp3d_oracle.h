@@ -20,11 +20,13 @@
  *   ORACLE_F64     the same discrete scheme evaluated entirely in double
  *                  (inputs promoted from float); used to state the FP32
  *                  rounding error of every result.
- *   ORACLE_MIRROR  FP32, the arithmetic the CUDA kernels perform (folded
- *                  1/dx coefficients, fused multiply-adds, Newton-Raphson
- *                  reciprocals in the scalar operator, IEEE square root),
- *                  written out operation by operation so that a correct
- *                  kernel matches it bit for bit.
+ *   ORACLE_MIRROR  FP32, the arithmetic the CUDA kernels perform in their
+ *                  fast mode (folded 1/dx coefficients, second differences
+ *                  in the reference's (u[+m] - 2u) + u[-m] form, fused
+ *                  multiply-adds, a Newton-Raphson reciprocal in the scalar
+ *                  operator, IEEE square root), written out operation by
+ *                  operation so that a correct kernel matches it bit for bit.
+ *                  The kernels' other mode reproduces ORACLE_REF32 itself.
  *
  * Parity pin: ORACLE_REF32 is checked bit-exact against the reference's own
  * CPU_function.c compiled from source (oracle/build.py); with that build

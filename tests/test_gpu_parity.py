@@ -1,4 +1,5 @@
-"""CUDA path against the oracle, through the C ABI (GPU).
+"""CUDA path in its default (fast) arithmetic against the oracle, through
+the C ABI (GPU).
 
 Three levels of agreement are checked:
   * bit for bit against the oracle's MIRROR variant -- the arithmetic the
@@ -7,10 +8,11 @@ Three levels of agreement are checked:
   * against the reference FP32 arithmetic (oracle REF32, pinned to
     CPU_function.c) and the golden vectors made by the reference's own code:
     relative L2 <= 1e-5 and max-abs <= 1e-4 of the peak;
-  * against FP64, stated for every result.
-The S operator switches on mode > 0.01*max|grad u| (GPU_kernel.cu:99); over
-long runs one-ulp differences flip cells across that threshold, so long-run
-bounds are the measured ones stated in the test.
+  * against FP64, relative L2 <= 1e-5 and stated for every result.
+The S operator switches on mode > 0.01*max|grad u| (GPU_kernel.cu:99), so any
+two FP32 arithmetics that are not bit-identical drift apart by threshold
+flips over long runs; the bounds hold over a whole 1000-step shot.  The
+reference-arithmetic mode is checked bit for bit in test_reference_arith.py.
 """
 import numpy as np
 import pytest
@@ -149,23 +151,22 @@ def test_small_shot_all_variants(ctx):
 
 def test_linear_vti_plain_shot_full(ctx):
     """100^3 interior, 20-cell PML, 1000 steps of 0.5 ms, 25 Hz Ricker at
-    (50,50,5), receivers on z=5: the reference CPU path's own workload.
-    Measured (oracle, this arithmetic): vs reference FP32 rel 1.54e-5,
-    max 3.8e-6 of peak; reference FP32 vs FP64 rel 6.9e-6.  The excess over
-    1e-5 rel is confined to the late, small-amplitude part of the record where
-    S-threshold flips dominate; the first 500 steps hold 1e-5."""
+    (50,50,5), receivers on z=5: the reference CPU path's own workload, in the
+    default (fast) arithmetic.  Bounds: relative L2 <= 1e-5 against the
+    reference FP32 arithmetic and against FP64 over the whole record, max-abs
+    <= 1e-4 of the peak.  (The reference's own GPU and CPU codes differ by
+    7.0e-6 on this shot; the reference-arithmetic mode equals the CPU code
+    bit for bit, test_reference_arith.py.)"""
     shot = synthetic.linear_vti()
     rec = ctx.forward(shot)
     r32, r64 = plain_shot_oracles(shot)
     e_rel, e_max = rel_l2(rec, r32), max_abs_rel_peak(rec, r32)
-    e_half = rel_l2(rec[:500], r32[:500])
     e64, e64_ref = rel_l2(rec, r64), rel_l2(r32, r64)
-    print("plain shot: vs ref32 rel %.3e max %.3e first-half rel %.3e | vs FP64 %.3e "
-          "(ref32 vs FP64 %.3e)" % (e_rel, e_max, e_half, e64, e64_ref))
-    assert e_max <= 1e-4
-    assert e_half <= 1e-5
-    assert e_rel <= 5e-5
-    assert e64 <= max(1e-5, 3 * e64_ref)
+    print("plain shot: vs ref32 rel %.3e max %.3e | vs FP64 %.3e max %.3e (ref32 vs FP64 %.3e)" %
+          (e_rel, e_max, e64, max_abs_rel_peak(rec, r64), e64_ref))
+    assert e_max <= 1e-4 and max_abs_rel_peak(rec, r64) <= 1e-4
+    assert e_rel <= 1e-5
+    assert e64 <= 1e-5
 
 
 # ---------------------------------------------------------------------------
