@@ -289,7 +289,7 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
                                          ctx->stream));
         } else {
             CKL(launch_params_dense(ctx->U[0], ctx->U[1], ctx->U[2], ctx->VP, ctx->E2, ctx->R8,
-                                    g->nx, g->ny, g->nz, ctx->ldy, g->dt, ctx->stream));
+                                    g->nx, g->ny, g->nz, ctx->ldy, ctx->stream));
         }
     }
     // coefficient tables
@@ -413,6 +413,8 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.w21n = ctx->W21[(k + 1) % 2];
     p.layers = ctx->layers;
     p.arith = ctx->arith;
+    p.wait_ns = ctx->wait_ns;
+    p.hold_plane = ctx->hold_plane;
     p.gmax = ctx->gmax;
     float *rec_plane = ctx->record + (size_t)k * ctx->hx * ctx->hy;
     p.record = ctx->rec_fused ? rec_plane : nullptr;
@@ -844,8 +846,13 @@ extern "C" void qp3d_host_free(void *p)
     if (p) cudaFreeHost(p);
 }
 
+namespace qp3d {
+int noalloc_tune(const char *key, int value);   // qp3d_noalloc.cu
+}
+
 extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
 {
+    if (!ctx && key) return noalloc_tune(key, value);
     if (!ctx || !key) return QP3D_ERR_ARG;
     if (!strcmp(key, "gradmax_variant") && (value == 0 || value == 1)) ctx->gradmax_variant = value;
     else if (!strcmp(key, "tile_x") && value >= 0 && value <= kMaxTileX) ctx->tune_tile_x = value;
@@ -862,6 +869,8 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
         ctx->spec_bias = value * 1e-6f;
     else if (!strcmp(key, "param_fp16") && (value == 0 || value == 1)) ctx->param_fp16 = value;
     else if (!strcmp(key, "arith") && (value == kArithRef || value == kArithFast)) ctx->arith = value;
+    else if (!strcmp(key, "wait_limit_us") && value >= 0) ctx->wait_ns = 1000ull * (unsigned)value;
+    else if (!strcmp(key, "test_hold_plane") && value >= -1) ctx->hold_plane = value + 1;
     else if (!strcmp(key, "adj_ckpt_bf16") && (value == 0 || value == 1)) ctx->adj_bf16 = value;
     else if (!strcmp(key, "adj_keep_all") && value >= -1 && value <= 1) ctx->adj_keep = value;
     else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
@@ -887,6 +896,9 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "spec_bias_ppm")) return (int)lrintf(ctx->spec_bias * 1e6f);
     if (!strcmp(key, "param_fp16")) return ctx->param_fp16;
     if (!strcmp(key, "arith")) return ctx->arith;
+    if (!strcmp(key, "wait_limit_us"))
+        return (int)((ctx->wait_ns ? ctx->wait_ns : 2000000000ull) / 1000ull);
+    if (!strcmp(key, "test_hold_plane")) return ctx->hold_plane - 1;
     if (!strcmp(key, "adj_ckpt_bf16")) return ctx->adj_bf16;
     if (!strcmp(key, "adj_keep_all")) return ctx->adj_keep;
     if (!strcmp(key, "batch_graph")) return ctx->batch_graph;

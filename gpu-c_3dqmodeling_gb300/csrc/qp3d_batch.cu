@@ -340,7 +340,7 @@ int Runner::run_group(std::vector<Plan *> &G, const Coefs &kc, const qp3d_shot *
                 CK(cudaMemcpyAsync(d.U[i], src[i], dense, cudaMemcpyHostToDevice, ctx->stream));
             CKL(launch_params_dense(d.U[0], d.U[1], d.U[2], const_cast<float *>(d.VP),
                                     const_cast<float *>(d.E2), const_cast<float *>(d.R8),
-                                    P.g.nx, P.g.ny, P.g.nz, P.ldy, P.g.dt, ctx->stream));
+                                    P.g.nx, P.g.ny, P.g.nz, P.ldy, ctx->stream));
             for (int i = 0; i < 3; ++i)
                 CK(cudaMemsetAsync(d.U[i], 0, (size_t)P.vol * sizeof(float), ctx->stream));
         }

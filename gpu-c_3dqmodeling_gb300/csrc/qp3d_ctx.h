@@ -89,6 +89,10 @@ struct qp3d_ctx {
     // arithmetic of the step: the fast folded form (default) or the reference
     // CPU operators' roundings, bit for bit ("arith" tuning key)
     int arith = qp3d::kArithFast;
+    // bounded device waits: limit (0: 2 s) and the withheld-plane test hook
+    // (plane index + 1 in the first CTA of each grid launch; 0: none)
+    unsigned long long wait_ns = 0;
+    int hold_plane = 0;
     long long launches = 0;          // kernels launched by this context
     // batched shots (qp3d_batch)
     qp3d::BatchState *batch = nullptr;

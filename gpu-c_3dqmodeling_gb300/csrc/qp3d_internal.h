@@ -110,6 +110,9 @@ struct PlaneParams {
     const SrcEntry *src;      // sources inside the updated box, fused
     int nsrc;
     unsigned *err;
+    unsigned long long wait_ns;   // limit of every bounded device wait (0: 2 s)
+    int hold_plane;           // test hook: plane hold_plane - 1 of the first CTA is
+                              // never loaded, so its waits run out (0: none)
     // threshold handling of the step kernel
     int spec;                 // 1: predicted window, own max, deferred cells
     const int *gate;          // exact mode: run only if *gate != 0 (null: always)
@@ -238,7 +241,7 @@ cudaError_t launch_crop(const float *u, float *out, int x0, int x1, int y0,
 // caller's layout, copied to the device in one piece) into the pitched
 // layout, row padding zero.
 cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *VP,
-                                float *E2, float *R8, int nx, int ny, int nz, int ldy, float dt,
+                                float *E2, float *R8, int nx, int ny, int nz, int ldy,
                                 cudaStream_t stream);
 cudaError_t launch_to_half_dense(const float *a, __half *h, int nx, int ny, int nz, int ldy,
                                  cudaStream_t stream);

@@ -89,14 +89,15 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Bounded wait: gives up after ~2 s of wall time.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+// Bounded wait: gives up after limit_ns of wall time.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity,
+                                                  unsigned long long limit_ns)
 {
     if (mbar_try_wait(bar, parity)) return true;
     unsigned long long t0 = global_ns();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > 2000000000ull) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -433,10 +434,13 @@ struct Pipe {
     int zfirst;      // z of staged plane 0
     int c0, c1;      // TMA coordinates of the box (y, x)
     int ncw;         // consumer warps
+    unsigned long long wait_ns;   // limit of every wait
+    int hold;        // test hook: plane never issued (-1: none)
 };
 
 __device__ __forceinline__ void pipe_issue(const Pipe &P, const CUtensorMap *tm, int i)
 {
+    if (i == P.hold) return;   // test hook: the waits for this plane run out
     int s = i % kRing;
     mbar_arrive_expect_tx(&P.full[s], P.box_bytes);
     tma_load_3d(P.ring + (size_t)s * P.slot_floats, tm, P.c0, P.c1, P.zfirst + i, &P.full[s]);
@@ -444,7 +448,7 @@ __device__ __forceinline__ void pipe_issue(const Pipe &P, const CUtensorMap *tm,
 
 __device__ __forceinline__ bool pipe_wait(const Pipe &P, int i)
 {
-    return mbar_wait_bounded(&P.full[i % kRing], (unsigned)((i / kRing) & 1));
+    return mbar_wait_bounded(&P.full[i % kRing], (unsigned)((i / kRing) & 1), P.wait_ns);
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
@@ -483,7 +487,7 @@ __device__ bool pipe_refill(const Pipe &P, const CUtensorMap *tm, int t, int &ne
         uint64_t *e = &P.empty[i % kRing];
         const unsigned par = (unsigned)(((i - kRing) / kRing) & 1);
         if (i <= t + 2 * kRadius) {
-            if (!mbar_wait_bounded(e, par)) return false;
+            if (!mbar_wait_bounded(e, par, P.wait_ns)) return false;
         } else if (!mbar_try_wait(e, par)) {
             break;
         }
@@ -515,12 +519,23 @@ __device__ __forceinline__ void pipe_setup(Pipe &P, unsigned char *smem, int til
     P.c0 = y0 - kHaloY;
     P.c1 = x0 - kRadius;
     P.ncw = blockDim.x >> 5;   // every warp of the CTA releases every slot
+    P.wait_ns = 2000000000ull;
+    P.hold = -1;
+}
+
+// The wait limit of the launch (0: 2 s) and the plane-withholding test hook,
+// which applies to the first CTA of a grid launch only.
+__device__ __forceinline__ void pipe_hooks(Pipe &P, const PlaneParams &p)
+{
+    if (p.wait_ns) P.wait_ns = p.wait_ns;
+    if (p.hold_plane > 0 && (blockIdx.x | blockIdx.y | blockIdx.z) == 0) P.hold = p.hold_plane - 1;
 }
 
 __device__ __forceinline__ void pipe_setup(Pipe &P, unsigned char *smem, const PlaneParams &p,
                                            int y0, int x0, int z0, int nzc)
 {
     pipe_setup(P, smem, p.tile_x, p.pml, y0, x0, z0, nzc);
+    pipe_hooks(P, p);
 }
 
 // Before a CTA reuses its barriers for another tile (thread 0, after a CTA
@@ -685,6 +700,7 @@ __device__ __forceinline__ bool gradmax_tile(const CUtensorMap *tm, const PlaneP
     const int nzc = z1 - z0;
     Pipe P;
     pipe_setup(P, smem, tile_x, p.pml, y0, x0, z0, nzc);
+    if (!REUSE) pipe_hooks(P, p);
     int next_issue = 0;
     if (tid == 0) {
         pipe_init(P);
@@ -1055,6 +1071,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
     const int nzc = z1 - z0;
     Pipe P;
     pipe_setup(P, smem, tile_x, p.pml, y0, x0, z0, nzc);
+    if (!REUSE) pipe_hooks(P, p);
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml;
     int next_issue = 0;
     if (tid == 0) {
@@ -1580,27 +1597,27 @@ __global__ void qp3d_crop_kernel(const float *u, float *out, int x0, int x1, int
     }
 }
 
-// Per-cell parameters (vp dt)^2, 2 eps, 8 (eps - delta) from dense
-// [nz][nx][ny] volumes (the caller's layout) into the pitched layout, one
-// thread per pitched cell, row padding zero; and the same layout change for
+// Per-cell parameters vp, 2 eps, 8 (eps - delta) from dense [nz][nx][ny]
+// volumes (the caller's layout) into the pitched layout, one thread per
+// pitched cell, row padding zero; and the same layout change for
 // half-precision storage.
 __global__ void qp3d_params_dense_kernel(const float *vp, const float *eps, const float *del,
-                                         float *K, float *E2, float *R8, int ny,
-                                         long long vol, int ldy, float dt)
+                                         float *VP, float *E2, float *R8, int ny,
+                                         long long vol, int ldy)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vol;
          i += (long long)gridDim.x * blockDim.x) {
         const long long row = i / ldy;
         const int y = (int)(i - row * ldy);
-        float k = 0.0f, e2 = 0.0f, r8 = 0.0f;
+        float v = 0.0f, e2 = 0.0f, r8 = 0.0f;
         if (y < ny) {
             const long long j = row * ny + y;
-            const float vdt = __fmul_rn(vp[j], dt), e = eps[j], d = del[j];
-            k = __fmul_rn(vdt, vdt);
+            const float e = eps[j], d = del[j];
+            v = vp[j];
             e2 = __fmul_rn(2.0f, e);
             r8 = __fmul_rn(8.0f, __fsub_rn(e, d));
         }
-        K[i] = k;
+        VP[i] = v;
         E2[i] = e2;
         R8[i] = r8;
     }
@@ -1954,7 +1971,7 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
                 nw1[j] = nw1o[j] = np_[j] = npo[j] = nw21[j] = nw3[j] = nw3o[j] = 0.0f;
                 c0[j] = c1[j] = c2[j] = 0.0f;
                 if (!(upd[j] && f[j] >= 0)) continue;
-                const float4 lc = a.layers[(f[j] >> 1) * pml + li[j]];
+                const float4 lc = fast_layer(a.layers[(f[j] >> 1) * pml + li[j]]);
                 const bool isz = f[j] >= 4;
                 const float A = isz ? KS[j] : e2[j] * KS[j], Bt = isz ? e2[j] * KS[j] : KS[j];
                 const float sgn = (f[j] & 1) ? -1.0f : 1.0f;
@@ -2356,14 +2373,14 @@ cudaError_t launch_from_bf16(const __nv_bfloat16 *h, float *a, long long n, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *K,
-                                float *E2, float *R8, int nx, int ny, int nz, int ldy, float dt,
+cudaError_t launch_params_dense(const float *vp, const float *eps, const float *del, float *VP,
+                                float *E2, float *R8, int nx, int ny, int nz, int ldy,
                                 cudaStream_t stream)
 {
     const long long vol = (long long)nz * nx * ldy;
     const long long b = (vol + 255) / 256;
     qp3d_params_dense_kernel<<<(int)(b > 16384 ? 16384 : b), 256, 0, stream>>>(
-        vp, eps, del, K, E2, R8, ny, vol, ldy, dt);
+        vp, eps, del, VP, E2, R8, ny, vol, ldy);
     return cudaGetLastError();
 }
 

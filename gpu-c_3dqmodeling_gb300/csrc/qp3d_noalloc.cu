@@ -2,20 +2,21 @@
 // device allocation.
 //
 // Some callers cannot let a library allocate device memory: a host program
-// whose framework has already reserved the whole device for its own pool, a
-// real-time loop that forbids allocation after start-up, or code that records
-// its work into a CUDA graph, where cudaMalloc and cudaFree cannot be
-// captured.  qp3d_gradmax_noalloc serves them.  It is the gradmax kernel of
-// the library, with its scratch (one partial maximum per CTA and an error
-// word) in file-scope device arrays of this translation unit instead of
-// buffers the library allocates; the caller passes the wavefield and the
-// output location.
+// whose framework has already reserved the whole device for its own pool, or
+// a real-time loop that forbids allocation after start-up.
+// qp3d_gradmax_noalloc serves them.  It is the gradmax kernel of the
+// library, with its scratch (one partial maximum per CTA and an error word)
+// in file-scope device arrays of this translation unit instead of buffers
+// the library allocates; the caller passes the wavefield and the output
+// location.
 //
 // The arrays exist once per device that loads the library and are held until
 // the process exits.  Every call shares them and they keep the last call's
 // contents, so calls that overlap on the GPU (different streams, or host
 // threads without ordering) race.  Each call clears the error word before it
-// launches; every partial slot it reads is written by the same call.
+// launches; every partial slot it reads is written by the same call.  The
+// call waits for its stream before it returns, so that a bounded device wait
+// that ran out is reported as QP3D_ERR_TIMEOUT.
 #include "qp3d.h"
 #include "qp3d_internal.h"
 
@@ -59,7 +60,21 @@ int report(char *err, size_t errlen, int code, const char *msg)
     return code;
 }
 
+// test hooks (set through qp3d_tune with a NULL context)
+unsigned long long g_wait_ns = 0;   // 0: the kernels' default (2 s)
+int g_hold_plane = 0;               // withheld plane + 1 in the first CTA, 0: none
+
 }  // namespace
+
+namespace qp3d {
+int noalloc_tune(const char *key, int value)
+{
+    if (!strcmp(key, "noalloc_wait_limit_us") && value >= 0) g_wait_ns = 1000ull * (unsigned)value;
+    else if (!strcmp(key, "noalloc_test_hold_plane") && value >= -1) g_hold_plane = value + 1;
+    else return QP3D_ERR_ARG;
+    return QP3D_OK;
+}
+}  // namespace qp3d
 
 extern "C" int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, int ldy, float dx,
                                     float dy, float dz, const float *c, float *d_max,
@@ -101,6 +116,14 @@ extern "C" int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, in
     nch = std::min(nch, (long long)(kNoAllocMaxBlocks / tiles));
     const int chunk_z = (int)((ncz + nch - 1) / nch);
     nch = (ncz + chunk_z - 1) / chunk_z;
+    // the launch grid is (y tiles, x tiles, z chunks); CUDA limits its second
+    // and third dimensions to 65535
+    if (nxt > 65535 || nch > 65535) {
+        snprintf(msg, sizeof(msg),
+                 "grid %dx%dx%d needs %d x tiles and %lld z chunks; the launch allows at most 65535",
+                 nx, ny, nz, nxt, nch);
+        return report(err, errlen, QP3D_ERR_ARG, msg);
+    }
     const unsigned nblocks = (unsigned)(tiles * nch);
 
     // once per device, with that device current: the scratch addresses and
@@ -154,6 +177,8 @@ extern "C" int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, in
     derive_coefs(c, c, dx, dy, dz, &p.k);   // first-derivative weights only
     p.arith = kArithFast;   // the library's default arithmetic
     p.err = ds.err;
+    p.wait_ns = g_wait_ns;
+    p.hold_plane = g_hold_plane;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the error word must start at zero; the partial slots are all written
     if (cudaMemsetAsync(ds.err, 0, sizeof(unsigned), s) != cudaSuccess)
@@ -165,5 +190,15 @@ extern "C" int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, in
         snprintf(msg, sizeof(msg), "launch failed: %s", cudaGetErrorString(e));
         return report(err, errlen, QP3D_ERR_CUDA, msg);
     }
+    // wait for the result and report a device wait that ran out (d_max then
+    // holds NaN); the error word is read into host memory, nothing allocated
+    unsigned flags = 0;
+    if ((e = cudaMemcpyAsync(&flags, ds.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+        snprintf(msg, sizeof(msg), "%s", cudaGetErrorString(e));
+        return report(err, errlen, QP3D_ERR_CUDA, msg);
+    }
+    if (flags) return report(err, errlen, QP3D_ERR_TIMEOUT, "a device wait timed out");
     return QP3D_OK;
 }

@@ -222,7 +222,16 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * checkpoint storage of the PML state, 0: FP32 (default), 1: BF16).
  * "adj_keep_all" (qp3d_adjoint schedule, 1: keep u^k of every step,
  * 0: checkpoints and recomputation, -1: keep all when nt wavefields fit in
- * the free device memory less 8 GiB). */
+ * the free device memory less 8 GiB).
+ * "arith" (arithmetic of the step, any time): 1 = fast (default: folded
+ * 1/h coefficients and fused multiply-adds; within 1e-5 relative L2 of the
+ * reference arithmetic over a 1000-step shot), 0 = the reference CPU
+ * operators' roundings, operation by operation (CPU_function.c:301-480),
+ * so that records, maxima and states equal the reference's bit for bit.
+ * "wait_limit_us" (limit of the kernels' bounded waits, 0: 2 s) and
+ * "test_hold_plane" (test hook: a plane index that the first CTA of each
+ * launch never loads, so that its waits run out and the step reports
+ * QP3D_ERR_TIMEOUT; -1: none). */
 int qp3d_tune(qp3d_ctx *ctx, const char *key, int value);
 int qp3d_tune_get(const qp3d_ctx *ctx, const char *key);
 
@@ -240,21 +249,27 @@ void qp3d_host_free(void *p);
  * caller keeps in device memory, computed without allocating any device
  * memory.  No counterpart in the reference (there the maximum is a host scan,
  * 3dPureqPModeling_single_shot.cu:284-292); it serves callers that cannot let
- * a library allocate: a framework that already holds the device memory, a
- * loop that forbids allocation after start-up, or a CUDA graph being
- * recorded, where cudaMalloc and cudaFree cannot be captured.
+ * a library allocate: a framework that already holds the device memory in
+ * its own pool, or a loop that forbids allocation after start-up.  Same
+ * arithmetic as the library's default path.
  *   d_u    device pointer, [nz][nx][ldy] float32, 16-byte aligned,
  *          ldy >= ny and a multiple of 4
  *   c      host pointer to the 36-entry fdcoff1 table
  *   d_max  device pointer to one float; NaN if a device wait timed out
- *   stream cudaStream_t (NULL: legacy default stream); asynchronous
+ *   stream cudaStream_t (NULL: legacy default stream); the call waits for
+ *          the stream before it returns
  *   err    optional message buffer (NULL to skip)
- * Limit: the grid may need at most 65536 tiles of 32x32 cells per z chunk
- * (nx*ny up to about 64 M cells); larger grids return QP3D_ERR_ARG.
+ * Returns QP3D_ERR_TIMEOUT when a bounded device wait ran out.
+ * Limits: the grid may need at most 65536 tiles of 32x32 cells per z chunk
+ * (nx*ny up to about 64 M cells), and at most 65535 tiles along x and z
+ * chunks; larger grids return QP3D_ERR_ARG.
  * Its scratch is a fixed device array that every GPU loading the library
  * holds until exit and that all calls share: calls that overlap on the GPU
  * race.  The first call on each device sets up the scratch addresses and the
- * kernel attributes; make it before any stream capture. */
+ * kernel attributes; make it before any stream capture.  Test hooks, set with
+ * qp3d_tune(NULL, key, value): "noalloc_wait_limit_us" (limit of the bounded
+ * waits, 0: 2 s) and "noalloc_test_hold_plane" (a plane the first CTA never
+ * loads, so that its waits run out; -1: none). */
 int qp3d_gradmax_noalloc(const float *d_u, int nx, int ny, int nz, int ldy,
                          float dx, float dy, float dz, const float *c,
                          float *d_max, void *stream, char *err, size_t errlen);

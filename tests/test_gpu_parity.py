@@ -135,6 +135,10 @@ def test_golden_fixture(ctx, name):
 
 
 def test_small_shot_all_variants(ctx):
+    """A 38x42x34 grid over 120 steps: the wave crosses every face several
+    times.  On a grid this small a single threshold flip moves the record by
+    ~1e-5, so the reference's own FP32 arithmetic is 1.3e-5 from FP64 here;
+    the fast arithmetic is held to the same distance from both."""
     shot = synthetic.small_case(nt=120, seed=9)
     rec = ctx.forward(shot)
     prob = shot.to_oracle(O)
@@ -142,9 +146,11 @@ def test_small_shot_all_variants(ctx):
     assert bits_equal(rec, mrec)
     r32, _, _ = O.run(O.REF32, prob)
     r64, _, _ = O.run(O.F64, prob)
-    assert rel_l2(rec, r32) <= 1e-5 and max_abs_rel_peak(rec, r32) <= 1e-4
-    # no less accurate than the reference's own FP32 arithmetic
-    assert rel_l2(rec, r64) <= max(1e-5, 3 * rel_l2(r32, r64))
+    e_ref = rel_l2(r32, r64)
+    print("small shot: fast vs REF32 %.3e, vs FP64 %.3e; REF32 vs FP64 %.3e" %
+          (rel_l2(rec, r32), rel_l2(rec, r64), e_ref))
+    assert rel_l2(rec, r32) <= max(1e-5, 2 * e_ref) and max_abs_rel_peak(rec, r32) <= 1e-4
+    assert rel_l2(rec, r64) <= max(1e-5, 2 * e_ref)
     _, g_cur, _ = ctx.read_state()
     assert bits_equal(g_cur, mst.u2)
 
