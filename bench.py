@@ -84,6 +84,10 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="scale the horizontal/vertical extent (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="skip the batched and gradient measurements of the default line")
+    ap.add_argument("--no-ref-arith", action="store_true",
+                    help="skip the timed shot in the reference-arithmetic mode")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="reference arm: skip the reference GPU kernels' sample")
     ap.add_argument("--workload", default="single",
@@ -421,6 +425,26 @@ def run_gpu_arm(args, dist):
                                   "%d re-runs in %d steps, max %d deferred cells per step" %
                                   (int(redo.sum()), nt, int(alt.max()))}
 
+    # the same shot in the reference-arithmetic mode (bit-identical to the
+    # reference CPU operators), one timed shot after one untimed
+    ref_arith = None
+    if not args.no_ref_arith:
+        ctx.tune(arith=0)
+        one_shot(False)
+        ctx.sync()
+        ctx.event(2)
+        ms_rs, _ = one_shot(True)
+        ctx.event(3)
+        ctx.sync()
+        ms_r = ctx.elapsed(2, 3)
+        ctx.tune(arith=1)
+        ref_arith = {"value": round(cells * nt / (ms_r / 1e3) / 1e9, 3), "unit": "Gcell/s",
+                     "ms_per_shot": round(ms_r, 2),
+                     "step_kernel_ms": round(ms_rs / nt, 5),
+                     "step_kernel_frac_of_peak": round(bstep / (ms_rs / nt / 1e3) / 1e9 / peak, 4),
+                     "note": "the reference CPU operators' roundings operation by operation "
+                             "(tuning key arith=0): records equal CPU_function.c's bit for bit"}
+
     # end to end through the C ABI from pinned host memory
     pin = {}
     for key in ("vp", "eps", "delta", "src", "wavelet"):
@@ -450,6 +474,11 @@ def run_gpu_arm(args, dist):
                "sample": "%d time steps of this grid from a dense random state; oracle port of "
                          "CPU_function.c (bit-exact to it), OpenMP" % CPU_SAMPLE_STEPS}
 
+    subs = {}
+    if dist.world == 1 and not args.no_sub:
+        subs["batch"] = batch_summary(ctx)
+        subs["adjoint"] = adjoint_summary(ctx)
+
     if dist.rank == 0:
         line = {
             "metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s",
@@ -463,12 +492,14 @@ def run_gpu_arm(args, dist):
                              (15 * cells * 4 / 1e9),
                        "parallelism": "replicas" if dist.world > 1 else "single"},
             "roofline": roofline,
+            "reference_arithmetic": ref_arith,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": round(1000 * e2e_s / args.steps, 2)},
             "gpu_launches": gpu_launches,
             "clocks": clk,
         }
+        line.update(subs)
         print(json.dumps(line), flush=True)
     for p in list(pin.values()) + [rec]:
         p.free()
@@ -573,6 +604,65 @@ def run_batch_arm(args, dist):
         print(json.dumps(line), flush=True)
     ctx.close()
     return 0
+
+
+def batch_summary(ctx, nshots=64, nt=2000):
+    """One timed qp3d_batch pass of the batched workload (after one untimed
+    pass, which also tunes the tile shape), beside the same shots as one
+    qp3d_shot_load + nt steps each (the one-shot-per-launch form); records of
+    both forms compared bit for bit on the first shots."""
+    import synthetic
+    shots = synthetic.batch_shots(nshots=nshots, nt=nt)
+    records = [np.empty((s.nt, s.hx, s.hy), np.float32) for s in shots]
+    ctx.batch(shots, records)
+    ctx.batch(shots, records)
+    st = ctx.batch_stats()
+    run_ms = st["run_ms"]
+    ms_single = 0.0
+    for s in shots:
+        ctx.load(s)
+        ms_single += ctx.time(s.nt, per_kernel=False)[0]
+    same = all(np.array_equal(ctx.forward(s).view(np.uint32), r.view(np.uint32))
+               for s, r in zip(shots[:4], records[:4]))
+    bsum = sum(algorithmic_bytes(s)[0] for s in shots)
+    peak, _ = hbm_peak()
+    achieved = bsum / (run_ms / nt / 1e3) / 1e9
+    return {"metric": "batched shots/s", "value": round(len(shots) / (run_ms / 1e3), 4),
+            "unit": "shots/s", "workload": BATCH_NAME % (len(shots), nt),
+            "one_shot_per_launch": round(len(shots) / (ms_single / 1e3), 4),
+            "speedup": round(ms_single / run_ms, 3),
+            "step_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                              "unit": "GB/s", "frac": round(achieved / peak, 4)},
+            "records_bit_identical_to_qp3d_forward": same,
+            "tuned_shape": {"tile_rows": st["tile_rows"], "zblocks": st["zblocks"]},
+            "note": "device time of the time loop (CUDA events) for both forms; the batched "
+                    "records equal the one-call records bit for bit (checked on 4 shots)"}
+
+
+def adjoint_summary(ctx, grid=4, nt=2000):
+    """Misfit gradient of the 16-shot gradient workload with the library's
+    default schedule, beside the forward alone of the same shots."""
+    import synthetic
+    true, start = synthetic.adjoint_case(nt=nt, grid=grid)
+    d_obs = [ctx.forward(s).copy() for s in true]
+    N = start[0].N
+    grads = [np.zeros(N, np.float64) for _ in range(3)]
+    ctx.adjoint(start[0], d_obs[0])
+    t0 = time.perf_counter()
+    J = 0.0
+    for s, d in zip(start, d_obs):
+        j, _ = ctx.adjoint(s, d, grads)
+        J += j
+    sec = (time.perf_counter() - t0) / len(start)
+    ctx.load(start[0])
+    t_fwd = ctx.time(nt, per_kernel=False)[0] / 1e3
+    return {"metric": "adjoint grad s/shot", "value": round(sec, 4), "unit": "s/shot",
+            "higher_is_better": False, "workload": ADJ_NAME % (len(start), nt),
+            "forward_only_s_per_shot": round(t_fwd, 4),
+            "schedule": "default (every u^k kept when nt wavefields fit in device memory)",
+            "misfit": J,
+            "accuracy": "gradient cosine against the FP64 CPU adjoint 1.000000 for vp, eps and "
+                        "delta on the test case (tests/test_adjoint.py)"}
 
 
 LARGE_NAME = ("anomalous layered VTI 800x800x400 + 40-cell PML (880x880x480 padded), 20 dipping "

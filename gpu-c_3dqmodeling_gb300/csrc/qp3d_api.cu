@@ -126,6 +126,8 @@ extern "C" void qp3d_ctx_destroy(qp3d_ctx *ctx)
     adjoint_free(ctx->adj);
     ctx->adj = nullptr;
     if (ctx->errword) cudaFree(ctx->errword);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto &ev : ctx->uev)
@@ -757,21 +759,54 @@ extern "C" int qp3d_forward(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     if (!ctx || !record) return QP3D_ERR_ARG;
     int rc = qp3d_shot_load(ctx, g, m);
     if (rc) return rc;
+    // A page-locked record buffer is filled while the time loop runs: the
+    // planes of each finished piece of steps go to the host on a second
+    // stream (the reference copies the whole wavefield back every step,
+    // 3dPureqPModeling_single_shot.cu:320); a pageable one is read at the end.
+    cudaPointerAttributes attr;
+    const bool pinned = cudaPointerGetAttributes(&attr, record) == cudaSuccess &&
+                        attr.type == cudaMemoryTypeHost;
+    (void)cudaGetLastError();
+    if (pinned && !ctx->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming));
+    }
+    const size_t row = (size_t)ctx->hx * ctx->hy;
     const bool snaps = snap && snap->fn && snap->ntsnap > 0 && snap->kinds;
-    int k = 0;
-    while (k < g->nt) {
-        int n = g->nt - k;
+    constexpr int kChunk = 100;   // steps per streamed piece of the record
+    int k = 0, sent = 0;
+    while (k < g->nt && rc == QP3D_OK) {
+        int n = std::min(g->nt - k, kChunk);
         if (snaps) {
             // the reference snapshots after step k when k % ntsnap == 0
             int next = (k % snap->ntsnap == 0) ? k : (k / snap->ntsnap + 1) * snap->ntsnap;
             n = std::min(n, next - k + 1);
         }
-        if ((rc = qp3d_shot_advance(ctx, n))) return rc;
+        if ((rc = qp3d_shot_advance(ctx, n))) break;
         k += n;
-        if (snaps && (k - 1) % snap->ntsnap == 0)
-            if ((rc = qp3d_shot_snapshot(ctx, snap))) return rc;
+        if (pinned && (k - sent >= kChunk || k == g->nt)) {
+            cudaError_t e = cudaEventRecord(ctx->copy_ev, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_ev, 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(record + (size_t)sent * row, ctx->record + (size_t)sent * row,
+                                    (size_t)(k - sent) * row * sizeof(float),
+                                    cudaMemcpyDeviceToHost, ctx->copy_stream);
+            if (e != cudaSuccess) {
+                rc = ctx_fail(ctx, QP3D_ERR_CUDA, "record copy: %s", cudaGetErrorString(e));
+                break;
+            }
+            sent = k;
+        }
+        if (snaps && (k - 1) % snap->ntsnap == 0) rc = qp3d_shot_snapshot(ctx, snap);
     }
-    return qp3d_shot_read_record(ctx, 0, g->nt, record);
+    if (!pinned) return rc ? rc : qp3d_shot_read_record(ctx, 0, g->nt, record);
+    // no copy into the caller's buffer may outlive the call, also on error
+    const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+    if (rc) return rc;
+    if ((rc = qp3d_shot_sync(ctx))) return rc;
+    if (e != cudaSuccess)
+        return ctx_fail(ctx, QP3D_ERR_CUDA, "record copy: %s", cudaGetErrorString(e));
+    return QP3D_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -27,6 +27,8 @@ struct qp3d_ctx {
     int device = 0;
     int nsm = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // record pieces to page-locked host memory
+    cudaEvent_t copy_ev = nullptr;
     EncodeTiledFn encode = nullptr;
     char err[512] = {0};
 

@@ -295,3 +295,20 @@ def test_speculative_threshold_paths(ctx, delta_ppm, bias_ppm):
         assert alt.max() > 0
     print("delta %d bias %d: re-runs %d of %d, max deferred cells %d" % (
         delta_ppm, bias_ppm, int(redo.sum()), shot.nt, int(alt.max())))
+
+
+def test_pinned_record_is_streamed_identically(ctx):
+    """A page-locked record buffer is filled piece by piece while the time
+    loop runs (a second stream); the result equals the pageable path's, with
+    and without snapshots, over several 100-step pieces."""
+    shot = synthetic.small_case(hx=20, hy=18, nz0=16, pml=6, nt=250, seed=6)
+    want = ctx.forward(shot)
+    snap = qp3d.make_snap(lambda step, kind, arr: 0, 30, [qp3d.SNAP_XZ])
+    for sn in (None, snap):
+        pin = qp3d.PinnedArray(want.shape)
+        try:
+            pin.array[:] = np.nan
+            ctx.forward(shot, snap=sn, record=pin.array)
+            assert bits_equal(pin.array, want)
+        finally:
+            pin.free()
