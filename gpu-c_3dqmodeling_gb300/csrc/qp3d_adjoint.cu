@@ -51,6 +51,7 @@ struct AdjState {
     void *ck = nullptr;            // nck checkpoints x 9 volumes
     float *resid = nullptr;        // nt * hx * hy: d_obs, then the residual
     float *T2 = nullptr;           // thresholds of a segment
+    unsigned *dec = nullptr;       // checkpoint schedule: every step's decisions
     double *misfit = nullptr;
 };
 
@@ -65,6 +66,7 @@ void adjoint_free(AdjState *s)
     cudaFree(s->ck);
     cudaFree(s->resid);
     cudaFree(s->T2);
+    cudaFree(s->dec);
     cudaFree(s->misfit);
     delete s;
 }
@@ -103,6 +105,11 @@ int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, int keep, 
     if (nck) CK(cudaMalloc(&s->ck, per * nck));
     CK(cudaMalloc(&s->resid, rec * sizeof(float)));
     CK(cudaMalloc(&s->T2, sizeof(float) * C));
+    if (nck) {   // one bit per cell and step: the forward's threshold decisions
+        const size_t db = (size_t)s->nt * (size_t)(s->vol / 32) * sizeof(unsigned);
+        CK(cudaMalloc(&s->dec, db));
+        CK(cudaMemset(s->dec, 0, db));
+    }
     CK(cudaMalloc(&s->misfit, sizeof(double)));
     s->C = C;
     s->nck = nck;
@@ -168,6 +175,21 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
                (j < 2 ? (size_t)j * vb : 2 * vb + (size_t)(j - 2) * hb);
     };
 
+    // The checkpoint schedule records every step's threshold decisions in the
+    // forward pass and replays them in the recomputation and the adjoint
+    // steps, so that a recomputation from rounded (BF16) checkpoints keeps
+    // the forward's S = 1 / anisotropic split; the decision is a
+    // discontinuity of S, and a flipped cell changes the delta gradient far
+    // more than the rounding itself.
+    struct DecGuard {
+        qp3d_ctx *c;
+        ~DecGuard() { c->dec_mode = 0; c->dec_base = nullptr; }
+    } dec_guard{ctx};
+    if (!keep) {
+        ctx->dec_base = S->dec;
+        ctx->dec_words = vol / 32;
+        ctx->dec_mode = 1;
+    }
     // ---- forward, keeping u^k or checkpoints
     for (int k = 0; k < nt; ++k) {
         if (keep) {
@@ -210,6 +232,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     for (int c = (keep ? 1 : nck) - 1; c >= 0; --c) {
         const int k0 = c * C, k1 = std::min(nt, k0 + C);
         if (!keep) {   // restore the checkpoint, recompute keeping u^k
+            ctx->dec_mode = 2;
             if ((rc = qp3d_internal_restore_step(ctx, k0))) return rc;
             float *v[9];
             live_state(ctx, k0, v);
@@ -231,6 +254,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
         CKL(launch_threshold(ctx->gmax + k0, S->T2, k1 - k0, ctx->stream));
         for (int k = k1 - 1; k >= k0; --k) {
             a.T2 = S->T2 + (k - k0);
+            a.dec = keep ? nullptr : S->dec + (size_t)k * (size_t)(vol / 32);
             a.u = S->seg + (size_t)(k - k0) * vol;
             a.resid = S->resid + (size_t)k * ctx->hx * ctx->hy;
             const float **Lc[9] = {&a.Lu, &a.Lup, &a.Lw1, &a.Lw1o, &a.Lp, &a.Lpo, &a.Lw21,

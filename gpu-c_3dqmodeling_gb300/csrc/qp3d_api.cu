@@ -379,7 +379,8 @@ constexpr int kSpecFirstStep = 3;
 
 static bool use_spec(const qp3d_ctx *ctx, int k)
 {
-    return ctx->threshold_mode == 1 && k >= kSpecFirstStep && ctx->vol < (1ll << 32);
+    return ctx->threshold_mode == 1 && ctx->dec_mode == 0 && k >= kSpecFirstStep &&
+           ctx->vol < (1ll << 32);
 }
 
 // Enqueue one time step.  ev_* are optional events bracketing the main step
@@ -417,6 +418,8 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
     p.arith = ctx->arith;
     p.wait_ns = ctx->wait_ns;
     p.hold_plane = ctx->hold_plane;
+    if (ctx->dec_mode == 1) p.dec_out = ctx->dec_base + (size_t)k * ctx->dec_words;
+    if (ctx->dec_mode == 2) p.dec_in = ctx->dec_base + (size_t)k * ctx->dec_words;
     p.gmax = ctx->gmax;
     float *rec_plane = ctx->record + (size_t)k * ctx->hx * ctx->hy;
     p.record = ctx->rec_fused ? rec_plane : nullptr;

@@ -95,6 +95,12 @@ struct qp3d_ctx {
     // (plane index + 1 in the first CTA of each grid launch; 0: none)
     unsigned long long wait_ns = 0;
     int hold_plane = 0;
+    // threshold decisions of each step (qp3d_adjoint): 1 = record them into
+    // dec_base + step * dec_words, 2 = replay them; steps then run exactly
+    // (gradmax pre-pass), not speculatively
+    int dec_mode = 0;
+    unsigned *dec_base = nullptr;
+    long long dec_words = 0;
     long long launches = 0;          // kernels launched by this context
     // batched shots (qp3d_batch)
     qp3d::BatchState *batch = nullptr;

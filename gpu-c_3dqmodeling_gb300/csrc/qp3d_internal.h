@@ -110,6 +110,11 @@ struct PlaneParams {
     const SrcEntry *src;      // sources inside the updated box, fused
     int nsrc;
     unsigned *err;
+    // threshold decisions of the step, one bit per cell in the layout of amask
+    // (exact steps only): written to dec_out, or read from dec_in instead of
+    // being taken (the gradient's recomputation replays the forward's)
+    unsigned *dec_out;
+    const unsigned *dec_in;
     unsigned long long wait_ns;   // limit of every bounded device wait (0: 2 s)
     int hold_plane;           // test hook: plane hold_plane - 1 of the first CTA is
                               // never loaded, so its waits run out (0: none)
@@ -199,6 +204,7 @@ struct AdjParams {
     const float *VP, *E2, *R8;             // vp, 2 eps, 8 (eps - delta)
     const float4 *layers;
     const float *T2;                       // threshold m2 of step k
+    const unsigned *dec;                   // or its decisions, one bit per cell (null: T2)
     const float *resid;                    // record residual of step k (hx * hy)
     const float *Lu, *Lup, *Lw1, *Lw1o, *Lp, *Lpo, *Lw21, *Lw3, *Lw3o;
     float *Nu, *Nup, *Nw1, *Nw1o, *Np, *Npo, *Nw21, *Nw3, *Nw3o;

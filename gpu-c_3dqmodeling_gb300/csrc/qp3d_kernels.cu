@@ -1193,6 +1193,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
             if (SPEC && cell_ok[j])
                 mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
             above[j] = m2[j] > T2lo;
+            if (!SPEC && p.dec_in && row_ok) above[j] = (p.dec_in[base >> 5] >> (4 * q + j)) & 1u;
             amb[j] = SPEC && cell_ok[j] && above[j] && !(m2[j] > T2hi);
             any_above = any_above || (row_ok && above[j]);
         }
@@ -1279,27 +1280,19 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                     }
                 } else {
                     const float4 lc = fast_layer(lt);
-                    float v;
-                    if (SPEC) {
-                        // also the S = 1 update of the cell and its split-field
-                        // outputs, kept for a deferred cell's fix-up (computing
-                        // both for every cell keeps the loop free of branches)
-                        float v1;
-                        float4 a1x;
-                        v = pml_cell2(f < 0 ? 0 : f, lc, KS[j],
-                                      __fmul_rn(k_of_vp(f4(Vv, j), dt), 1.0f), e1[j], Ux[j],
-                                      Uy[j], Uz[j], Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j),
-                                      f4(w12, j), f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
-                                      f4(p2, j), n13[j], n21[j], n33[j], n3[j], v1, a1x);
-                        if (is_pml && amb[j]) {
-                            alt[j] = v1;
-                            p.apml[base + j] = a1x;
-                        }
-                    } else {
-                        v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e1[j], Ux[j], Uy[j], Uz[j],
-                                     Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
-                                     f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j), f4(p2, j),
-                                     n13[j], n21[j], n33[j], n3[j]);
+                    const float v = pml_cell(f < 0 ? 0 : f, lc, KS[j], e1[j], Ux[j], Uy[j], Uz[j],
+                                             Uxx[j], Uyy[j], Uzz[j], dt, f4(w11, j), f4(w12, j),
+                                             f4(w21, j), f4(w31, j), f4(w32, j), f4(p1, j),
+                                             f4(p2, j), n13[j], n21[j], n33[j], n3[j]);
+                    if (SPEC && is_pml && amb[j]) {
+                        // the S = 1 update of a deferred cell and its split-field
+                        // outputs, kept for the fix-up
+                        float a13, a21, a33, a3;
+                        alt[j] = pml_cell(f, lc, __fmul_rn(k_of_vp(f4(Vv, j), dt), 1.0f), e1[j],
+                                          Ux[j], Uy[j], Uz[j], Uxx[j], Uyy[j], Uzz[j], dt,
+                                          f4(w11, j), f4(w12, j), f4(w21, j), f4(w31, j),
+                                          f4(w32, j), f4(p1, j), f4(p2, j), a13, a21, a33, a3);
+                        p.apml[base + j] = make_float4(a13, a21, a33, a3);
                     }
                     out[j] = is_pml ? v : out[j];
                     n13[j] = is_pml ? n13[j] : 0.0f;
@@ -1352,6 +1345,19 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                         p.record[(long long)(x - pml) * hy + (y - pml)] = out[j];
                 }
             }
+        }
+        // the step's decisions, when asked for (same word layout as the
+        // deferred-cell mask below)
+        if (!SPEC && p.dec_out) {
+            const unsigned nib = (unsigned)(cell_ok[0] && above[0]) |
+                                 ((unsigned)(cell_ok[1] && above[1]) << 1) |
+                                 ((unsigned)(cell_ok[2] && above[2]) << 2) |
+                                 ((unsigned)(cell_ok[3] && above[3]) << 3);
+            unsigned w = nib << (4 * q);
+            w |= __shfl_xor_sync(0xffffffffu, w, 1);
+            w |= __shfl_xor_sync(0xffffffffu, w, 2);
+            w |= __shfl_xor_sync(0xffffffffu, w, 4);
+            if (q == 0 && row_ok) p.dec_out[base >> 5] = w;
         }
         // deferred cells: the row's bitmask word (the 8 lanes of a row combine
         // their 4 bits; written every step, so stale bits never survive), and
@@ -1926,7 +1932,9 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
             const float h2 = fmaf(Uy[j], Uy[j], Ux[j] * Ux[j]), m2 = fmaf(Uz[j], Uz[j], h2);
             S[j] = 1.0f;
             dSe[j] = dSd[j] = 0.0f;
-            if (m2 > T2) {
+            const bool on = a.dec ? ((a.dec[i >> 5] >> ((unsigned)(i & 31) + j)) & 1u) != 0
+                                  : (m2 > T2);
+            if (on) {
                 const float aa = __fdividef(h2, m2), bb = 1.0f - aa, D = fmaf(E2, aa, 1.0f);
                 const float iD = __fdividef(1.0f, D);
                 const float ab8 = 8.0f * aa * bb * iD * iD;

@@ -113,3 +113,29 @@ def test_adjoint_against_live_finite_differences(reference):
           % (an, fd, abs(an - fd) / abs(fd)))
     # the frozen operator leaves out dS/du (measured 4.6 % on this case)
     assert abs(an - fd) <= 0.10 * abs(fd)
+
+
+def test_bf16_checkpoints_at_reduced_gradient_workload():
+    """The gradient workload at reduced size (the 12-layer model of the
+    16-shot case at 100x100x75 cells + 20-cell PML, a start model smoothed
+    by sigma = 2.5 cells, 2x2 shots, 800 steps): sqrt(nt) checkpoints with the
+    PML levels in BF16 and the forward's threshold decisions replayed, against
+    every u^k kept in FP32 (the schedule checked against the FP64 adjoint
+    above): cosine >= 0.999 for vp, eps and delta."""
+    true, start = synthetic.adjoint_case(hx=100, hy=100, nz0=75, pml=20, nt=800, sigma=2.5,
+                                         grid=2)
+    out = {}
+    with qp3d.Context(0) as ctx:
+        d_obs = [ctx.forward(s).copy() for s in true]
+        for name, bf16, keep in (("bf16", 1, 0), ("fp32", 0, 0), ("keep", 0, 1)):
+            ctx.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
+            grads = [np.zeros(start[0].N, np.float64) for _ in range(3)]
+            for s, d in zip(start, d_obs):
+                ctx.adjoint(s, d, grads)
+            out[name] = grads
+    for a, b in zip(out["fp32"], out["keep"]):
+        assert np.array_equal(a, b)
+    for name, a, b in zip(("vp", "eps", "delta"), out["bf16"], out["keep"]):
+        c = _cos(a, b)
+        print("reduced gradient workload, BF16 PML checkpoints %s: cosine %.6f" % (name, c))
+        assert c >= 0.999, (name, c)
