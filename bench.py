@@ -14,8 +14,13 @@ Metric: Gcell-updates/s = padded cells x time steps / seconds.
   e2e        the same shots through qp3d_forward (the modeling3d replacement)
              from pinned host buffers: model upload, time loop, record download
   roofline   the fused step kernel: algorithmic bytes per launch
-             (24 B per interior cell + 64 B per PML cell) / its mean duration,
-             against the measured HBM copy bandwidth
+             (24 B per interior cell + 64 B per PML cell) / its mean duration
+             (CUDA events around every launch of one more shot, outside the
+             timed shots), against the measured HBM copy bandwidth
+  reference_arithmetic  one shot in the reference-arithmetic mode (arith=0),
+             whose records equal the reference CPU operators' bit for bit
+  batch, adjoint  one timed pass of the batched and gradient workloads below
+             (default line, one GPU)
   cpu_baseline  the reference CPU arithmetic (oracle port of CPU_function.c,
              bit-exact to it) on all host cores, on a bounded sample
 
@@ -386,11 +391,8 @@ def run_gpu_arm(args, dist):
     clocks = Clocks(gpu_index)
     launches0 = ctx.launch_count()
     ctx.event(0)
-    ms_step, ms_grad = 0.0, 0.0
     for _ in range(args.steps):
-        a, b = one_shot(True)
-        ms_step += a
-        ms_grad += b
+        one_shot(False)
     ctx.event(1)
     ctx.sync()
     ms = ctx.elapsed(0, 1)
@@ -400,10 +402,13 @@ def run_gpu_arm(args, dist):
     value = dist.world * cells * nt * args.steps / (ms / 1e3) / 1e9
     gpu_launches = ctx.launch_count() - launches0
     redo, alt = ctx.stats(0, nt)
+    # the step kernel's own duration: one more shot with events around every
+    # launch (kept out of the timed shots, whose loop it would slow)
+    ms_step, ms_grad = one_shot(True)
 
     # roofline of the fused step kernel (one launch = one time step)
     bstep, ni, np_ = algorithmic_bytes(shot)
-    n_launch = nt * args.steps
+    n_launch = nt
     t_step = ms_step / n_launch / 1e3
     achieved = bstep / t_step / 1e9
     peak, peak_kind = hbm_peak()
@@ -425,6 +430,29 @@ def run_gpu_arm(args, dist):
                                   "%d re-runs in %d steps, max %d deferred cells per step" %
                                   (int(redo.sum()), nt, int(alt.max()))}
 
+    # end to end through the C ABI from pinned host memory
+    pin = {}
+    for key in ("vp", "eps", "delta", "src", "wavelet"):
+        a = getattr(shot, key)
+        pa = qp3d.PinnedArray(a.shape)
+        pa.array[:] = a
+        pin[key] = pa
+    rec = qp3d.PinnedArray((nt, shot.hx, shot.hy))
+    pshot = qp3d.Shot(shot.nx, shot.ny, shot.nz, shot.pml, shot.sz, shot.dx, shot.dy, shot.dz,
+                      shot.dt, pin["vp"].array, pin["eps"].array, pin["delta"].array,
+                      pin["src"].array, pin["wavelet"].array, shot.prof, shot.c, shot.c2)
+    ctx.forward(pshot, snap=snap, record=rec.array)     # warm-up
+    dist.barrier()
+    clocks_e2e = Clocks(gpu_index)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.forward(pshot, snap=snap, record=rec.array)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    clk_e2e = clocks_e2e.stop()
+    e2e = dist.world * cells * nt * args.steps / e2e_s / 1e9
+    h2d = 3 * cells * 4 + nt * 4 + 6 * shot.pml * 4 + 2 * 36 * 4
+    d2h = nt * shot.hx * shot.hy * 4 + snaps_per_shot * (shot.nz - 2 * shot.pml) * (shot.hx + shot.hy) * 4
+
     # the same shot in the reference-arithmetic mode (bit-identical to the
     # reference CPU operators), one timed shot after one untimed
     ref_arith = None
@@ -444,27 +472,6 @@ def run_gpu_arm(args, dist):
                      "step_kernel_frac_of_peak": round(bstep / (ms_rs / nt / 1e3) / 1e9 / peak, 4),
                      "note": "the reference CPU operators' roundings operation by operation "
                              "(tuning key arith=0): records equal CPU_function.c's bit for bit"}
-
-    # end to end through the C ABI from pinned host memory
-    pin = {}
-    for key in ("vp", "eps", "delta", "src", "wavelet"):
-        a = getattr(shot, key)
-        pa = qp3d.PinnedArray(a.shape)
-        pa.array[:] = a
-        pin[key] = pa
-    rec = qp3d.PinnedArray((nt, shot.hx, shot.hy))
-    pshot = qp3d.Shot(shot.nx, shot.ny, shot.nz, shot.pml, shot.sz, shot.dx, shot.dy, shot.dz,
-                      shot.dt, pin["vp"].array, pin["eps"].array, pin["delta"].array,
-                      pin["src"].array, pin["wavelet"].array, shot.prof, shot.c, shot.c2)
-    ctx.forward(pshot, snap=snap, record=rec.array)     # warm-up
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ctx.forward(pshot, snap=snap, record=rec.array)
-    e2e_s = dist.max(time.perf_counter() - t0)
-    e2e = dist.world * cells * nt * args.steps / e2e_s / 1e9
-    h2d = 3 * cells * 4 + nt * 4 + 6 * shot.pml * 4 + 2 * 36 * 4
-    d2h = nt * shot.hx * shot.hy * 4 + snaps_per_shot * (shot.nz - 2 * shot.pml) * (shot.hx + shot.hy) * 4
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -495,7 +502,11 @@ def run_gpu_arm(args, dist):
             "reference_arithmetic": ref_arith,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": round(1000 * e2e_s / args.steps, 2)},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(1000 * e2e_s / args.steps, 2),
+                    "clocks": clk_e2e,
+                    "note": "qp3d_forward from page-locked host buffers, every step: the "
+                            "parameter volumes to the device, the time loop, the record "
+                            "streamed back during the loop and the xz/yz slices"},
             "gpu_launches": gpu_launches,
             "clocks": clk,
         }
@@ -641,19 +652,32 @@ def batch_summary(ctx, nshots=64, nt=2000):
 
 def adjoint_summary(ctx, grid=4, nt=2000):
     """Misfit gradient of the 16-shot gradient workload with the library's
-    default schedule, beside the forward alone of the same shots."""
+    default schedule (every u^k kept when they fit in device memory), and
+    with the sqrt(nt) checkpoint schedule in its default storage (BF16 PML
+    levels, the forward's threshold decisions replayed), beside the forward
+    alone of the same shots; the checkpointed gradient's cosine against the
+    kept one (FP32 checkpoints give the kept gradient bit for bit)."""
     import synthetic
     true, start = synthetic.adjoint_case(nt=nt, grid=grid)
     d_obs = [ctx.forward(s).copy() for s in true]
     N = start[0].N
-    grads = [np.zeros(N, np.float64) for _ in range(3)]
-    ctx.adjoint(start[0], d_obs[0])
-    t0 = time.perf_counter()
-    J = 0.0
-    for s, d in zip(start, d_obs):
-        j, _ = ctx.adjoint(s, d, grads)
-        J += j
-    sec = (time.perf_counter() - t0) / len(start)
+
+    def run(keep):
+        ctx.tune(adj_keep_all=keep)
+        grads = [np.zeros(N, np.float64) for _ in range(3)]
+        ctx.adjoint(start[0], d_obs[0])
+        t0 = time.perf_counter()
+        J = 0.0
+        for s, d in zip(start, d_obs):
+            j, _ = ctx.adjoint(s, d, grads)
+            J += j
+        return (time.perf_counter() - t0) / len(start), J, grads
+
+    sec, J, g_keep = run(-1)
+    sec_ck, J_ck, g_ck = run(0)
+    ctx.tune(adj_keep_all=-1)
+    cos = [float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b)))
+           for a, b in zip(g_ck, g_keep)]
     ctx.load(start[0])
     t_fwd = ctx.time(nt, per_kernel=False)[0] / 1e3
     return {"metric": "adjoint grad s/shot", "value": round(sec, 4), "unit": "s/shot",
@@ -661,6 +685,11 @@ def adjoint_summary(ctx, grid=4, nt=2000):
             "forward_only_s_per_shot": round(t_fwd, 4),
             "schedule": "default (every u^k kept when nt wavefields fit in device memory)",
             "misfit": J,
+            "checkpointed": {"s_per_shot": round(sec_ck, 4), "misfit": J_ck,
+                             "schedule": "ceil(sqrt(nt)) checkpoints, PML levels in BF16, "
+                                         "threshold decisions of the forward replayed",
+                             "cosine_vs_kept": {"vp": round(cos[0], 6), "eps": round(cos[1], 6),
+                                                "delta": round(cos[2], 6)}},
             "accuracy": "gradient cosine against the FP64 CPU adjoint 1.000000 for vp, eps and "
                         "delta on the test case (tests/test_adjoint.py)"}
 

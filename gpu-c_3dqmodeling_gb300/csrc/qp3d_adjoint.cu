@@ -14,20 +14,23 @@
 // (240x240x190 padded cells x 2000 steps is 88 GB) the forward pass keeps
 // every u^k and the backward pass runs straight through.  Otherwise the
 // forward pass stores the state every C = ceil(sqrt(nt)) steps (nine volumes:
-// u, u_prev and the seven live PML levels), in FP32 by default so that the
-// recomputation is bit-identical to the forward; the backward pass restores
+// u, u_prev and the seven live PML levels) and the backward pass restores
 // each checkpoint, recomputes its C steps keeping u^k, and runs the C adjoint
-// steps backward.  With "adj_ckpt_bf16" the PML levels are kept
-// in BF16 (22 instead of 36 bytes per cell and checkpoint); u always stays
-// FP32 because S depends on the direction of grad u, a difference of
-// neighbouring values that BF16 rounding of a smooth wavefield destroys.  The
-// delta gradient lives in S, whose threshold decision is a discontinuity, so
-// it is the component most sensitive to any change of the recomputed
-// wavefield (measured on 16 shots of 240x240x190: cosine against FP32
-// checkpoints 0.999999 vp, 0.99997 eps, 0.91 delta with BF16 PML levels,
-// 0.87 delta with an all-BF16 state).  Device memory:
-// ~27 volumes plus nt (all kept) or C volumes and the checkpoints.  Gradients are summed per shot in
-// FP32 on the device and added to the caller's FP64 arrays.
+// steps backward.  By default ("adj_ckpt_bf16" = 1) the seven PML levels of a
+// checkpoint are stored in BF16 (22 instead of 36 bytes per cell and
+// checkpoint) and the forward pass also records every step's threshold
+// decisions (one bit per cell and step), which the recomputation replays
+// instead of re-deciding: the rounded PML levels then change the recomputed
+// wavefield by rounding-sized amounts but never flip a decision of S, whose
+// threshold is a discontinuity of the operator and dominated the delta
+// gradient's error without the replay (cosine against FP32 checkpoints 0.91
+// on 16 shots of 240x240x190).  u and u_prev stay FP32: S depends on the
+// direction of grad u, a difference of neighbouring values that BF16
+// rounding of a smooth wavefield would destroy.  With "adj_ckpt_bf16" = 0 the
+// checkpoints are FP32 and the recomputation is bit-identical to the forward.
+// Device memory: ~27 volumes plus nt (all kept) or C volumes, the checkpoints
+// and nt/32 volumes of decision bits.  Gradients are summed per shot in FP32
+// on the device and added to the caller's FP64 arrays.
 #include "qp3d_ctx.h"
 
 #include <algorithm>

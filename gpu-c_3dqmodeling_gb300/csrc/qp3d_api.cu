@@ -45,7 +45,7 @@ static void free_shot(qp3d_ctx *ctx)
                       &ctx->R8,    &ctx->W1[0], &ctx->W1[1], &ctx->W1[2], &ctx->W3[0],
                       &ctx->W3[1], &ctx->W3[2], &ctx->P[0],  &ctx->P[1],  &ctx->P[2],
                       &ctx->W21[0], &ctx->W21[1], &ctx->record, &ctx->gmax, &ctx->snap_dev,
-                      &ctx->win,   &ctx->spec_err, &ctx->am2, &ctx->av, &ctx->sres};
+                      &ctx->win,   &ctx->spec_err, &ctx->am2, &ctx->av};
     for (float **b : bufs) {
         if (*b) cudaFree(*b);
         *b = nullptr;
@@ -270,7 +270,6 @@ extern "C" int qp3d_shot_load(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_mode
         CK(cudaMalloc(&ctx->av, (size_t)ctx->vol * sizeof(float)));
         CK(cudaMalloc(&ctx->apml, (size_t)ctx->vol * sizeof(float4)));
         CK(cudaMalloc(&ctx->fix_count, ntb * sizeof(unsigned)));
-        CK(cudaMalloc(&ctx->sres, 2 * ntb * sizeof(float)));
         // compacted list: a quarter of the cells (more deferred cells than
         // that make the step re-run exactly)
         ctx->alist_cap = (unsigned)std::min<long long>(std::max(1ll << 16, ctx->vol / 4), 0x7fffffff);
@@ -442,17 +441,15 @@ static int enqueue_step(qp3d_ctx *ctx, cudaEvent_t ev_g0, cudaEvent_t ev_g1, cud
         p.alist = ctx->alist;
         p.alist_cap = ctx->alist_cap;
         p.fix_count = ctx->fix_count + k;
-        p.sres = ctx->sres + 2 * (size_t)k;
         if (ev_s0) CK(cudaEventRecord(ev_s0, ctx->stream));
         CKL(launch_step(ctx->tm[a], p, grid, ctx->smem, ctx->stream));
         if (ev_s1) CK(cudaEventRecord(ev_s1, ctx->stream));
         if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
-        CKL(launch_fixup(p, ctx->redo + k, ctx->spec_err, ctx->stream, ctx->nsm));
-        ctx->launches += 2;   // resolution, compaction, fix-up
+        CKL(launch_compact(p, ctx->redo + k, ctx->spec_err, ctx->stream));
         PlaneParams pe = p;
         pe.spec = 0;
         pe.gate = ctx->redo + k;
-        CKL(launch_step(ctx->tm[a], pe, grid, ctx->smem, ctx->stream));
+        CKL(launch_fix_or_rerun(ctx->tm[a], pe, ctx->nsm, ctx->smem, ctx->stream));
         if (ev_g1) CK(cudaEventRecord(ev_g1, ctx->stream));
     } else {
         if (ev_g0) CK(cudaEventRecord(ev_g0, ctx->stream));
@@ -497,7 +494,6 @@ int qp3d_internal_restore_step(qp3d_ctx *ctx, int step)
     CK(cudaMemsetAsync(ctx->redo + step, 0, n * sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->alt_count + step, 0, n * sizeof(unsigned), ctx->stream));
     CK(cudaMemsetAsync(ctx->fix_count + step, 0, n * sizeof(unsigned), ctx->stream));
-    CK(cudaMemsetAsync(ctx->sres + 2 * (size_t)step, 0, 2 * n * sizeof(float), ctx->stream));
     ctx->step = step;
     ctx->cur = (3 - step % 3) % 3;
     ctx->prev = (ctx->cur + 1) % 3;
@@ -507,7 +503,7 @@ int qp3d_internal_restore_step(qp3d_ctx *ctx, int step)
 extern "C" int qp3d_shot_launches_per_step(const qp3d_ctx *ctx)
 {
     if (!ctx || !ctx->loaded) return 0;
-    int n = use_spec(ctx, ctx->step) ? 5 : 2;   // step, resolution, compaction, fix-up, re-run
+    int n = use_spec(ctx, ctx->step) ? 3 : 2;   // step, compaction, fix-up or re-run
     if (ctx->fuse_sources) n += ctx->n_band > 0 ? 1 : 0;
     else n += ctx->n_all > 0 ? 1 : 0;
     if (!ctx->rec_fused) n += 1;

@@ -36,7 +36,7 @@ struct Cand {
 };
 constexpr Cand kCands[] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}};
 constexpr int kNumCands = (int)(sizeof(kCands) / sizeof(kCands[0]));
-constexpr int kDefaultCand = 1;
+constexpr int kDefaultCand = 4;   // 16 rows: three CTAs per SM
 constexpr int kTuneSteps = 2;       // steps per candidate and pass (two passes)
 constexpr int kGraphSteps = 8;      // steps per captured graph
 constexpr int kSpecFirst = 3;       // as the single-shot path
@@ -119,7 +119,6 @@ void carve(Plan &s, Carver &c, size_t *zero_bytes)
     d.redo = c.take<int>(nt);
     d.alt_count = c.take<unsigned>(nt);
     d.fix_count = c.take<unsigned>(nt);
-    d.sres = c.take<float>(2 * nt);
     d.amask = c.take<unsigned>((size_t)defer_mask_words((long long)vol));
     if (zero_bytes) *zero_bytes = c.off - start;
     d.VP = c.take<float>(vol);
@@ -271,7 +270,7 @@ int Runner::enqueue_step(int c, bool spec)
         CKL(launch_batch_plane(2, args(c, 1), l.grid, l.threads, l.smem, ctx->stream));
         const int per_shot = std::max(2, 8 * ctx->nsm / std::max(nshots, 1));
         CKL(launch_batch_fixup(args(c, 1), nshots, per_shot, max_words, ctx->stream));
-        ctx->launches += 2;   // resolution, compaction, fix-up
+        ctx->launches += 1;   // compaction and fix-up
         CKL(launch_batch_plane(1, args(c, 2), l.grid, l.threads, l.smem, ctx->stream));
     } else {
         CKL(launch_batch_plane(0, args(c, 0), l.grid, l.threads, l.smem, ctx->stream));

@@ -57,7 +57,6 @@ struct qp3d_ctx {
     float *am2 = nullptr, *av = nullptr;
     float4 *apml = nullptr;
     unsigned *fix_count = nullptr;   // per step: deferred cells below the threshold
-    float *sres = nullptr;           // per step: T2 and the window hit
     unsigned *alist = nullptr;       // compacted deferred cells
     unsigned alist_cap = 0;
     float4 *layers = nullptr;
@@ -110,7 +109,7 @@ struct qp3d_ctx {
     long long batch_mem_mb = 0;      // device memory for one group of shots, 0: auto
     // adjoint (qp3d_adjoint)
     qp3d::AdjState *adj = nullptr;
-    int adj_bf16 = 0;                // 1: PML levels of the checkpoints in BF16
+    int adj_bf16 = 1;                // 1: PML levels of the checkpoints in BF16
     int adj_keep = -1;               // 1: keep every u^k, 0: checkpoints, -1: by free memory
 };
 inline int ctx_fail(qp3d_ctx *c, int code, const char *fmt, ...)

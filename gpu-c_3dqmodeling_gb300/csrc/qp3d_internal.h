@@ -135,7 +135,6 @@ struct PlaneParams {
     float4 *apml;
     unsigned *alt_count;      // &alt_count[step]: deferred cells (compaction)
     unsigned *fix_count;      // &fix_count[step]: of them below the threshold
-    float *sres;              // &sres[2*step]: T2 of the true max, 1 if inside the window
     unsigned *alist;          // their pitched indices (compaction -> fix-up)
     unsigned alist_cap;
     // batched launches only
@@ -167,7 +166,6 @@ struct BatchShot {
     float *am2, *av;          // vol each
     float4 *apml;             // vol
     unsigned *fix_count;      // nt
-    float *sres;              // 2 * nt
     unsigned *alist;          // alist_cap entries
     unsigned alist_cap;
     float spec_bias;
@@ -227,8 +225,12 @@ cudaError_t launch_step(const CUtensorMap &tm_u, const PlaneParams &p,
                         dim3 grid, size_t smem, cudaStream_t stream);
 // Speculative step resolution: compaction of the deferred-cell bitmask into a
 // list, then the fix-up of the listed cells.
-cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
-                         int nsm);
+// resolution and compaction of a speculative step, then its fix-up or (when
+// the max fell outside the window) its exact re-run, a persistent grid of
+// nsm CTAs
+cudaError_t launch_compact(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream);
+cudaError_t launch_fix_or_rerun(const CUtensorMap &tm_u, const PlaneParams &p, int nsm,
+                                size_t smem, cudaStream_t stream);
 cudaError_t launch_band_sources(float *u_new, const float *u_cur,
                                 const SrcEntry *src, int n, long long plane,
                                 int ldy, float w, cudaStream_t stream);

@@ -1409,43 +1409,36 @@ __global__ void __launch_bounds__(kThreads, 2)
                                      blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0, smem);
 }
 
-// Resolution of a speculative step, one thread: whether the true max fell in
-// the predicted window, the threshold T2 of the true max, the re-run flag and
-// the relative error of the prediction.
-__device__ __forceinline__ void resolve_body(const PlaneParams &p, int *redo, float *spec_err)
-{
-    const float M = p.gmax[p.step];
-    const float lo = p.win[0], hi = p.win[1], pred = p.win[2];
-    const bool inside = (M >= lo) && (M <= hi);
-    p.sres[0] = threshold_m2(M);
-    p.sres[1] = inside ? 1.0f : 0.0f;
-    *redo = inside ? 0 : 1;   // the fix-up sets it too when the list overflows
-#pragma unroll
-    for (int i = kSpecHist - 1; i > 0; --i) spec_err[i] = spec_err[i - 1];
-    spec_err[0] = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
-}
-
-__global__ void qp3d_resolve_kernel(const PlaneParams p, int *redo, float *spec_err)
-{
-    if (threadIdx.x == 0) resolve_body(p, redo, spec_err);
-}
-
-// Compaction of the deferred-cell bitmask, four words per thread, one global
-// atomic per block and counter.  *p.alt_count ends as the number of deferred
-// cells of the step; when the true max lies in the predicted window, the
-// cells that are below the true threshold (m2 <= T2) are listed in p.alist
-// and counted in *p.fix_count.
-__device__ __forceinline__ void compact_body(const PlaneParams &p, unsigned block)
+// Resolution and compaction of a speculative step, over the deferred-cell
+// bitmask (four words per thread).  Every block derives from the true max M
+// whether it fell in the predicted window and the threshold T2 of M (thread 0,
+// while the others load their words); block 0 also sets the re-run flag and
+// shifts the history of the prediction's relative errors.  *p.alt_count ends as the number of deferred
+// cells of the step; when M is inside the window, the deferred cells below
+// the threshold are listed in p.alist and counted in *p.fix_count.
+__device__ __forceinline__ void compact_body(const PlaneParams &p, unsigned block, int *redo,
+                                             float *spec_err)
 {
     __shared__ unsigned s_warp[32], s_def[32];
     __shared__ unsigned s_base;
-    const float T2 = p.sres[0];
-    const bool inside = p.sres[1] != 0.0f;
+    const float M = p.gmax[p.step];   // complete: the step kernel has finished
+    const bool inside = (M >= p.win[0]) && (M <= p.win[1]);
+    __shared__ float s_T2;
+    if (threadIdx.x == 0) s_T2 = threshold_m2(M);
+    if (block == 0 && threadIdx.x == 0) {
+        *redo = inside ? 0 : 1;   // the fix-up sets it too when the list overflows
+        const float pred = p.win[2];
+#pragma unroll
+        for (int i = kSpecHist - 1; i > 0; --i) spec_err[i] = spec_err[i - 1];
+        spec_err[0] = pred > 0.0f ? fabsf(__fdiv_rn(M, pred) - 1.0f) : 1.0f;
+    }
     const unsigned nwords = (unsigned)defer_mask_words(p.plane * p.nz);   // a multiple of 4
     const unsigned w0 = (block * blockDim.x + threadIdx.x) * 4u;
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint4 wv = make_uint4(0u, 0u, 0u, 0u);
     if (w0 < nwords) wv = *reinterpret_cast<const uint4 *>(p.amask + w0);
+    __syncthreads();
+    const float T2 = s_T2;
     const unsigned ws[4] = {wv.x, wv.y, wv.z, wv.w};
     unsigned fix[4] = {0u, 0u, 0u, 0u};
     unsigned c = 0, dcnt = 0;
@@ -1502,25 +1495,21 @@ __device__ __forceinline__ void compact_body(const PlaneParams &p, unsigned bloc
     }
 }
 
-__global__ void qp3d_compact_kernel(const PlaneParams p) { compact_body(p, blockIdx.x); }
-
-// Fix-up of a speculative step.  If the true max lies in the window and the
-// list did not overflow, every listed cell (deferred and below the true
-// threshold) gets the S = 1 results the step kernel stored for it (u(k+1),
-// and at PML cells the split-field state); otherwise *redo = 1 (set here or
-// by the resolution) and the gated exact re-run recomputes the whole step.
-__device__ __forceinline__ void fixup_body(const PlaneParams &p, int *redo, unsigned block,
-                                           unsigned nblocks)
+__global__ void qp3d_compact_kernel(const PlaneParams p, int *redo, float *spec_err)
 {
-    const unsigned n = *p.fix_count;
-    if (p.sres[1] == 0.0f) return;   // window missed: the step re-runs
-    if (n > p.alist_cap) {            // list overflow: re-run as well
-        if (block == 0 && threadIdx.x == 0) *redo = 1;
-        return;
-    }
+    compact_body(p, blockIdx.x, redo, spec_err);
+}
+
+// Fix-up of a speculative step: every listed cell (deferred and below the
+// true threshold) gets the S = 1 results the step kernel stored for it
+// (u(k+1), and at PML cells the split-field state).  Only called when the max
+// fell in the window and the list did not overflow.
+__device__ __forceinline__ void fixup_cells(const PlaneParams &p, unsigned n, unsigned first,
+                                            unsigned stride)
+{
     const int nx = p.nx, ny = p.ny, nz = p.nz, pml = p.pml, hy = ny - 2 * pml;
     const unsigned plane = (unsigned)p.plane, ldy = (unsigned)p.ldy;
-    for (unsigned i = block * blockDim.x + threadIdx.x; i < n; i += nblocks * blockDim.x) {
+    for (unsigned i = first; i < n; i += stride) {
         const unsigned idx = p.alist[i];
         const int z = (int)(idx / plane);
         const unsigned rem = idx - (unsigned)z * plane;
@@ -1541,9 +1530,36 @@ __device__ __forceinline__ void fixup_body(const PlaneParams &p, int *redo, unsi
     }
 }
 
-__global__ void qp3d_fixup_kernel(const PlaneParams p, int *redo)
+// The fix-up of a speculative step, or its exact re-run when the max fell
+// outside the predicted window (*p.gate, set by the compaction) or the list
+// overflowed: one persistent grid of one CTA per SM.  The re-run takes the
+// step's tile columns in turn, so a step that needs none costs one short
+// wave instead of a full grid of CTAs that each read the gate and exit.
+template <bool HALF, int AR>
+__global__ void __launch_bounds__(kThreads, 1)
+    qp3d_fix_or_rerun_kernel(const __grid_constant__ CUtensorMap tm_u, const PlaneParams p)
 {
-    fixup_body(p, redo, blockIdx.x, gridDim.x);
+    const unsigned n = *p.fix_count;
+    const bool rerun = *p.gate != 0 || n > p.alist_cap;
+    if (!rerun) {
+        fixup_cells(p, n, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *const_cast<int *>(p.gate) = 1;   // overflow: count it
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int nyt = (p.ny - kRadius - 1) / kTileY + 1;
+    const int nxt = (p.nx - 2 * kRadius + p.tile_x - 1) / p.tile_x;
+    const int nch = (p.nz - 2 * kRadius + p.chunk_z - 1) / p.chunk_z;
+    const int ntiles = nyt * nxt * nch;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int by = t % nyt, bx = (t / nyt) % nxt, bz = t / (nyt * nxt);
+        const int z0 = kRadius + bz * p.chunk_z;
+        const int z1 = min(z0 + p.chunk_z, p.nz - kRadius);
+        if (z0 >= z1) continue;
+        if (!step_tile<false, true, HALF, AR>(&tm_u, p, p.k, p.tile_x, by * kTileY,
+                                              kRadius + bx * p.tile_x, z0, z1, false, smem))
+            return;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1654,7 +1670,8 @@ __global__ void qp3d_to_half_dense_kernel(const float *a, __half *h, int ny, lon
 //                               shot -- from an atomic queue and run the
 //                               gradmax or step tile body on it; uneven shot
 //                               sizes mix in one launch.
-//   qp3d_batch_fixup_kernel     the speculative fix-up, blockIdx.y = shot.
+//   qp3d_batch_compact_kernel,  the speculative resolution, compaction
+//   qp3d_batch_fixup_kernel     and fix-up, blockIdx.y = shot.
 // ---------------------------------------------------------------------------
 __global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, PlaneParams *pp,
                                           int *ctr, int *queues, int spec)
@@ -1702,7 +1719,6 @@ __global__ void qp3d_batch_prepare_kernel(const BatchShot *shots, int nshots, Pl
             p.alist = b.alist;
             p.alist_cap = b.alist_cap;
             p.fix_count = b.fix_count + k;
-            p.sres = b.sres + 2 * (long long)k;
         }
         pp[s] = p;
     }
@@ -1721,9 +1737,13 @@ size_t batch_smem_bytes(int tile_x, int pml, int nsrc)
 }
 
 // KIND 0: gradmax, 1: exact step (skipped for shots whose gate is 0),
-// 2: speculative step.
+// 2: speculative step.  Bounded for one CTA of kThreads per SM: the per-shot
+// parameters live in shared memory rather than in the constant bank, and held
+// to the two-CTA budget of 128 registers the step body spills (measured: 15 %
+// fewer shots/s).  The shape tuner then picks the tile height, which sets how
+// many CTAs share an SM (three of 128 threads at 16 rows).
 template <int KIND, int AR>
-__global__ void __launch_bounds__(kThreads, 2) qp3d_batch_plane_kernel(const __grid_constant__ BatchArgs b)
+__global__ void __launch_bounds__(kThreads, 1) qp3d_batch_plane_kernel(const __grid_constant__ BatchArgs b)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     // item slot double-buffered by iteration: thread 0 can run one iteration
@@ -1775,28 +1795,26 @@ __global__ void __launch_bounds__(kThreads, 2) qp3d_batch_plane_kernel(const __g
     }
 }
 
-__global__ void qp3d_batch_resolve_kernel(const __grid_constant__ BatchArgs b, int nshots)
-{
-    for (int s = threadIdx.x; s < nshots; s += blockDim.x) {
-        const PlaneParams &p = b.pp[s];
-        if (p.active && p.spec)
-            resolve_body(p, const_cast<int *>(p.gate), const_cast<float *>(p.spec_err));
-    }
-}
-
 __global__ void qp3d_batch_compact_kernel(const __grid_constant__ BatchArgs b)
 {
     const PlaneParams &p = b.pp[blockIdx.y];
     if (!p.active || !p.spec) return;
     if ((long long)blockIdx.x * blockDim.x * 4 >= defer_mask_words(p.plane * p.nz)) return;
-    compact_body(p, blockIdx.x);
+    compact_body(p, blockIdx.x, const_cast<int *>(p.gate), const_cast<float *>(p.spec_err));
 }
 
+// Fix-up of the shots whose max fell in their window; a shot whose list
+// overflowed is marked for the exact pass instead.
 __global__ void qp3d_batch_fixup_kernel(const __grid_constant__ BatchArgs b)
 {
     const PlaneParams &p = b.pp[blockIdx.y];
-    if (!p.active || !p.spec) return;
-    fixup_body(p, const_cast<int *>(p.gate), blockIdx.x, gridDim.x);
+    if (!p.active || !p.spec || *p.gate) return;
+    const unsigned n = *p.fix_count;
+    if (n > p.alist_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *const_cast<int *>(p.gate) = 1;
+        return;
+    }
+    fixup_cells(p, n, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -2170,7 +2188,9 @@ cudaError_t configure_kernels()
         (e = set_smem(qp3d_step_kernel<false, false, AR>, bytes)) ||                        \
         (e = set_smem(qp3d_step_kernel<true, true, AR>, bytes)) ||                          \
         (e = set_smem(qp3d_step_kernel<false, true, AR>, bytes)) ||                         \
-        (e = set_smem(qp3d_gradmax_kernel<false, AR>, bytes)))                              \
+        (e = set_smem(qp3d_gradmax_kernel<false, AR>, bytes)) ||                            \
+        (e = set_smem(qp3d_fix_or_rerun_kernel<false, AR>, bytes)) ||                              \
+        (e = set_smem(qp3d_fix_or_rerun_kernel<true, AR>, bytes)))                                 \
         return e;
     QP3D_STEP_SMEM(kArithFast)
     QP3D_STEP_SMEM(kArithRef)
@@ -2238,16 +2258,28 @@ cudaError_t launch_gradmax_partial(const CUtensorMap &tm_u, const PlaneParams &p
     return cudaGetLastError();
 }
 
-cudaError_t launch_fixup(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream,
-                         int nsm)
+cudaError_t launch_compact(const PlaneParams &p, int *redo, float *spec_err, cudaStream_t stream)
 {
     const long long words = defer_mask_words(p.plane * p.nz);
-    qp3d_resolve_kernel<<<1, 32, 0, stream>>>(p, redo, spec_err);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    qp3d_compact_kernel<<<(unsigned)((words / 4 + 255) / 256), 256, 0, stream>>>(p);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    qp3d_fixup_kernel<<<8 * nsm, 256, 0, stream>>>(p, redo);
+    qp3d_compact_kernel<<<(unsigned)((words / 4 + 255) / 256), 256, 0, stream>>>(p, redo,
+                                                                                 spec_err);
+    return cudaGetLastError();
+}
+
+template <int AR>
+static void launch_fix_or_rerun_t(const CUtensorMap &tm_u, const PlaneParams &p, int grid, int t,
+                                  size_t smem, cudaStream_t stream)
+{
+    if (p.half_params) qp3d_fix_or_rerun_kernel<true, AR><<<grid, t, smem, stream>>>(tm_u, p);
+    else qp3d_fix_or_rerun_kernel<false, AR><<<grid, t, smem, stream>>>(tm_u, p);
+}
+
+cudaError_t launch_fix_or_rerun(const CUtensorMap &tm_u, const PlaneParams &p, int nsm,
+                                size_t smem, cudaStream_t stream)
+{
+    const int t = plane_threads(p.tile_x);
+    if (p.arith == kArithRef) launch_fix_or_rerun_t<kArithRef>(tm_u, p, nsm, t, smem, stream);
+    else launch_fix_or_rerun_t<kArithFast>(tm_u, p, nsm, t, smem, stream);
     return cudaGetLastError();
 }
 
@@ -2288,12 +2320,10 @@ cudaError_t launch_batch_plane(int kind, const BatchArgs &b, int grid, int threa
 cudaError_t launch_batch_fixup(const BatchArgs &b, int nshots, int blocks_per_shot,
                                long long max_words, cudaStream_t stream)
 {
-    qp3d_batch_resolve_kernel<<<1, 128, 0, stream>>>(b, nshots);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
     qp3d_batch_compact_kernel<<<dim3((unsigned)((max_words / 4 + 255) / 256), nshots), 256, 0,
                                 stream>>>(b);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     qp3d_batch_fixup_kernel<<<dim3(blocks_per_shot, nshots), 256, 0, stream>>>(b);
     return cudaGetLastError();
 }

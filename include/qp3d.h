@@ -149,10 +149,12 @@ int qp3d_batch_get_stats(const qp3d_ctx *ctx, qp3d_batch_stats *out);
  * all nt wavefields fit in device memory the forward keeps them
  * ("adj_keep_all", default -1: decided by free memory), otherwise it stores
  * checkpoints every ceil(sqrt(nt)) steps and the backward recomputes each
- * segment, bit-identically with FP32 checkpoints (default);
- * "adj_ckpt_bf16" = 1 keeps the seven PML state levels in BF16 (u and u_prev
- * stay FP32), which perturbs mostly the delta gradient.  Both schedules give
- * the same gradient bit for bit with FP32 checkpoints.  The gradient is added (+=) to the caller's padded [nz][nx][ny]
+ * segment.  By default ("adj_ckpt_bf16" = 1) a checkpoint keeps the seven PML
+ * state levels in BF16 (u and u_prev stay FP32) and the recomputation replays
+ * the forward's threshold decisions, recorded as one bit per cell and step;
+ * with "adj_ckpt_bf16" = 0 the checkpoints are FP32 and the recomputation is
+ * bit-identical to the forward, so that both schedules give the same
+ * gradient bit for bit.  The gradient is added (+=) to the caller's padded [nz][nx][ny]
  * FP64 arrays on the cells outside the PML shell (the shell's parameters
  * extend the interior edge and are held fixed); NULL skips one.  misfit:
  * out, J (may be NULL).  Needs FP32 parameter storage and sources and
@@ -219,7 +221,8 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * vp, epsilon and delta as IEEE half, rounded to nearest; the stencil stays
  * FP32, and the results equal an FP32 run on the rounded model bit for bit;
  * qp3d_batch always stores FP32).  "adj_ckpt_bf16" (qp3d_adjoint
- * checkpoint storage of the PML state, 0: FP32 (default), 1: BF16).
+ * checkpoint storage of the PML state, 0: FP32, 1: BF16 with the forward's
+ * threshold decisions replayed (default)).
  * "adj_keep_all" (qp3d_adjoint schedule, 1: keep u^k of every step,
  * 0: checkpoints and recomputation, -1: keep all when nt wavefields fit in
  * the free device memory less 8 GiB).

@@ -126,6 +126,7 @@ def test_bf16_checkpoints_at_reduced_gradient_workload():
                                          grid=2)
     out = {}
     with qp3d.Context(0) as ctx:
+        assert ctx.tuning("adj_ckpt_bf16") == 1      # the default storage
         d_obs = [ctx.forward(s).copy() for s in true]
         for name, bf16, keep in (("bf16", 1, 0), ("fp32", 0, 0), ("keep", 0, 1)):
             ctx.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
