@@ -425,8 +425,9 @@ def run_gpu_arm(args, dist):
                 "step_kernel_ms": round(ms_step / n_launch, 5),
                 "threshold_overhead_ms": round(ms_grad / n_launch, 5),
                 "threshold_note": "per step: gradmax pre-pass for the first 3 steps, then the "
-                                  "resolution, deferred-cell compaction and fix-up kernels and "
-                                  "the gated exact re-run of the speculative step; last shot: "
+                                  "resolution and deferred-cell compaction kernel and the "
+                                  "fix-up (or, when the max left the window, the exact re-run) "
+                                  "of the speculative step; last shot: "
                                   "%d re-runs in %d steps, max %d deferred cells per step" %
                                   (int(redo.sum()), nt, int(alt.max()))}
 
@@ -444,11 +445,22 @@ def run_gpu_arm(args, dist):
     ctx.forward(pshot, snap=snap, record=rec.array)     # warm-up
     dist.barrier()
     clocks_e2e = Clocks(gpu_index)
+    per_shot = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        t1 = time.perf_counter()
         ctx.forward(pshot, snap=snap, record=rec.array)
+        per_shot.append(round((time.perf_counter() - t1) * 1e3, 1))
     e2e_s = dist.max(time.perf_counter() - t0)
     clk_e2e = clocks_e2e.stop()
+    # its parts: the upload and set-up of the model (qp3d_shot_load from the
+    # same page-locked buffers), after which the time loop and the record run
+    load_ms = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        ctx.load(pshot)
+        ctx.sync()
+        load_ms.append((time.perf_counter() - t1) * 1e3)
     e2e = dist.world * cells * nt * args.steps / e2e_s / 1e9
     h2d = 3 * cells * 4 + nt * 4 + 6 * shot.pml * 4 + 2 * 36 * 4
     d2h = nt * shot.hx * shot.hy * 4 + snaps_per_shot * (shot.nz - 2 * shot.pml) * (shot.hx + shot.hy) * 4
@@ -503,6 +515,7 @@ def run_gpu_arm(args, dist):
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": round(1000 * e2e_s / args.steps, 2),
+                    "ms_per_shot": per_shot, "load_ms": round(min(load_ms), 1),
                     "clocks": clk_e2e,
                     "note": "qp3d_forward from page-locked host buffers, every step: the "
                             "parameter volumes to the device, the time loop, the record "
