@@ -36,6 +36,9 @@ Nz0 in [128, 200], 20-cell PML, 10.8 M padded cells on average) cut from one
              (model upload, time loop, record download)
   single_shot_form  the same shots one qp3d call each: device time of the
              resident time loop and wall time of qp3d_forward
+Under torchrun with N ranks the shots are split into N contiguous blocks
+balanced by cells x steps (shard.py), one qp3d_batch call per rank; value =
+all shots / the slowest rank's time ("strong" scaling).
 
 --workload adjoint measures the misfit gradient (qp3d_adjoint): a 12-layer
 200x200x150 true model (+20-cell PML, 240x240x190 padded) and a start model
@@ -44,7 +47,10 @@ steps, sqrt(nt) checkpoints in FP32 (and with BF16 PML levels beside it);
 value = seconds per shot of the gradient (forward, residual, checkpointed
 backward), the records of the true model made first.  Beside it, the schedule
 that keeps every u^k in device memory (88 GB here, no recomputation; the
-library's default when it fits), whose gradient is identical.
+library's default when it fits), whose gradient is identical.  Under
+torchrun the shots are split into contiguous blocks across ranks and the FP64
+gradient is summed on the host in shot order, bit-equal to one process
+(shard.py).
 
 --workload large measures the large mixed-precision configuration (one bench
 step = one shot): 800x800x400 cells + 40-cell PML (880x880x480 padded, 372 M
@@ -539,33 +545,41 @@ BATCH_NAME = ("%d shots, windows hx,hy U[128,256], Nz0 U[128,200] (+20-cell PML)
 def run_batch_arm(args, dist):
     import qp3d
     import synthetic
+    import shard
     nt = args.nt if args.nt is not None else 2000
-    shots = synthetic.batch_shots(nshots=args.shots, nt=nt)
-    cells = [s.N for s in shots]
+    all_shots = synthetic.batch_shots(nshots=args.shots, nt=nt)
+    # ranks take contiguous blocks of the shot list, balanced by cells x steps
+    blocks = shard.partition([shard.shot_cost(s) for s in all_shots], dist.world)
+    a, b = blocks[dist.rank]
+    shots = all_shots[a:b]
+    cells = [s.N for s in all_shots]
     work = sum(c * nt for c in cells)
     ctx = qp3d.Context(dist.local)
     if args.spec_delta_ppm is not None:
         ctx.tune(spec_delta_ppm=args.spec_delta_ppm)
     records = [np.empty((s.nt, s.hx, s.hy), np.float32) for s in shots]
     for _ in range(args.warmup):
-        ctx.batch(shots, records)
+        if shots:
+            ctx.batch(shots, records)
     dist.barrier()
     gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
     clocks = Clocks(gpu_index)
     launches0 = ctx.launch_count()
     run_ms, wall = 0.0, 0.0
+    st = {}
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        ctx.batch(shots, records)
+        if shots:
+            ctx.batch(shots, records)
+            st = ctx.batch_stats()
+            run_ms += st["run_ms"]
         wall += time.perf_counter() - t0
-        st = ctx.batch_stats()
-        run_ms += st["run_ms"]
     clk = clocks.stop()
     gpu_launches = ctx.launch_count() - launches0
     run_ms = dist.max(run_ms)
     wall = dist.max(wall)
-    n = dist.world * len(shots) * args.steps
+    n = len(all_shots) * args.steps
     value = n / (run_ms / 1e3)
     e2e = n / wall
 
@@ -578,49 +592,56 @@ def run_batch_arm(args, dist):
     for s, r in zip(shots, records):
         ctx.forward(s, record=r)
     wall_single = time.perf_counter() - t0
+    ms_single = dist.max(ms_single)
+    wall_single = dist.max(wall_single)
 
     # whole-step HBM rate of the batched time loop (algorithmic bytes of all
     # shots per step / device time per step)
-    bsum = sum(algorithmic_bytes(s)[0] for s in shots)
+    bsum = sum(algorithmic_bytes(s)[0] for s in all_shots)
     peak, peak_kind = hbm_peak()
     achieved = bsum / (run_ms / args.steps / nt / 1e3) / 1e9
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
-        secs, threads = cpu_sample(shots[0], CPU_SAMPLE_STEPS, k0=nt // 2)
-        rate = shots[0].N * CPU_SAMPLE_STEPS / secs
-        cpu = {"value": round(rate / (work / len(shots)), 6), "unit": "shots/s", "cores": threads,
+        secs, threads = cpu_sample(all_shots[0], CPU_SAMPLE_STEPS, k0=nt // 2)
+        rate = all_shots[0].N * CPU_SAMPLE_STEPS / secs
+        cpu = {"value": round(rate / (work / len(all_shots)), 6), "unit": "shots/s",
+               "cores": threads,
                "kind": "port",
                "sample": "%d time steps of shot 0 (%dx%dx%d) from a dense random state, oracle "
                          "port of CPU_function.c, OpenMP; shots/s = cell rate / mean cells x nt"
-                         % (CPU_SAMPLE_STEPS, shots[0].nx, shots[0].ny, shots[0].nz)}
+                         % (CPU_SAMPLE_STEPS, all_shots[0].nx, all_shots[0].ny,
+                            all_shots[0].nz)}
     if dist.rank == 0:
         line = {
             "metric": "batched shots/s", "value": round(value, 4), "unit": "shots/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(run_ms / args.steps, 2), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": BATCH_NAME % (len(shots), nt),
-                       "step": "one qp3d_batch call over all shots",
-                       "shots": len(shots), "nt": nt, "cells_total": sum(cells),
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": BATCH_NAME % (len(all_shots), nt),
+                       "step": "one qp3d_batch call per rank over its block of the shots",
+                       "shots": len(all_shots), "nt": nt, "cells_total": sum(cells),
                        "cells_mean": round(sum(cells) / len(cells)),
                        "l2": "inputs larger than L2 (working set %.0f GB)" %
                              (sum(17 * c * 4 for c in cells) / 1e9),
-                       "parallelism": "replicas" if dist.world > 1 else "single"},
-            "gcell_per_s": round(dist.world * work * args.steps / (run_ms / 1e3) / 1e9, 3),
+                       "parallelism": ("shots split into %d contiguous blocks balanced by "
+                                       "cells x steps, one per rank, no exchange"
+                                       % dist.world) if dist.world > 1 else "single",
+                       "blocks": blocks},
+            "gcell_per_s": round(work * args.steps / (run_ms / 1e3) / 1e9, 3),
             "step_roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                               "unit": "GB/s", "frac": round(achieved / peak, 4),
                               "note": "algorithmic bytes of all shots per time step / device "
                                       "time per step (all kernels of the step)"},
             "batch": st,
             "single_shot_form": {
-                "value": round(len(shots) / (ms_single / 1e3), 4), "unit": "shots/s",
-                "e2e": round(len(shots) / wall_single, 4),
+                "value": round(len(all_shots) / (ms_single / 1e3), 4), "unit": "shots/s",
+                "e2e": round(len(all_shots) / wall_single, 4),
                 "note": "same shots, one call each: device time of the resident time loop "
                         "(qp3d_shot_load + nt steps), and wall time of qp3d_forward"},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e, 4), "unit": "shots/s",
                     "h2d_bytes_per_step": sum(4 * (3 * c) + 4 * nt for c in cells),
-                    "d2h_bytes_per_step": sum(4 * nt * s.hx * s.hy for s in shots),
+                    "d2h_bytes_per_step": sum(4 * nt * s.hx * s.hy for s in all_shots),
                     "note": "pageable host buffers"},
             "gpu_launches": gpu_launches,
             "clocks": clk,
@@ -797,30 +818,37 @@ def run_adjoint_arm(args, dist):
     import synthetic
     nt = args.nt if args.nt is not None else 2000
     grid = 4 if args.shots >= 16 else max(1, int(round(args.shots ** 0.5)))   # grid x grid shots
+    import shard
     true, start = synthetic.adjoint_case(nt=nt, grid=grid)
+    # ranks take contiguous blocks of the shots; the FP64 gradient is summed
+    # across them in shot order (bit-equal to one process)
+    blocks = shard.partition([shard.shot_cost(s) for s in start], dist.world)
+    a, b = blocks[dist.rank]
     ctx = qp3d.Context(dist.local)
-    d_obs = [ctx.forward(s).copy() for s in true]
-    N = start[0].N
+    d_obs = {i: ctx.forward(true[i]).copy() for i in range(a, b)}
     res = {}
     gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
+
+    def one_shot(i, s, out):
+        J, _ = ctx.adjoint(s, d_obs[i], out)
+        return J
+
     clocks = Clocks(gpu_index)
     launches0 = ctx.launch_count()
     for name, bf16, keep in (("fp32_checkpoints", 0, 0), ("bf16_pml_checkpoints", 1, 0),
                              ("keep_all", 0, 1)):
         ctx.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
         for _ in range(args.warmup):
-            ctx.adjoint(start[0], d_obs[0])
-        grads = [np.zeros(N, np.float64) for _ in range(3)]
-        J = 0.0
+            if b > a:
+                ctx.adjoint(start[a], d_obs[a])
+        dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            for s, d in zip(start, d_obs):
-                j, _ = ctx.adjoint(s, d, grads)
-                J += j
-        sec = time.perf_counter() - t0
+            J, grads = shard.gradient(start, one_shot)
+        sec = dist.max(time.perf_counter() - t0)
         res[name] = {"s_per_shot": round(sec / (args.steps * len(start)), 4),
-                     "misfit": J / args.steps, "grads": grads}
+                     "misfit": J, "grads": grads}
     clk = clocks.stop()
     gpu_launches = ctx.launch_count() - launches0
     cos = {}
@@ -829,8 +857,7 @@ def run_adjoint_arm(args, dist):
         cos[p] = round(float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b))), 6)
     keep_same = all(np.array_equal(a, b) for a, b in zip(res["keep_all"]["grads"],
                                                           res["fp32_checkpoints"]["grads"]))
-    t_fwd = None
-    ctx.load(start[0])
+    ctx.load(start[a] if b > a else start[0])
     tot, _, _ = ctx.time(nt, per_kernel=False)
     t_fwd = tot / 1e3
     if dist.rank == 0:
@@ -839,12 +866,16 @@ def run_adjoint_arm(args, dist):
             "unit": "s/shot", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * res["fp32_checkpoints"]["s_per_shot"]
                                                         * len(start), 1),
-            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "higher_is_better": False, "scaling": "strong", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
             "config": {"workload": ADJ_NAME % (len(start), nt),
                        "step": "gradient of all %d shots" % len(start),
                        "grid": [start[0].nx, start[0].ny, start[0].nz], "nt": nt,
-                       "parallelism": "single"},
+                       "parallelism": ("shots split into %d contiguous blocks, one per rank; "
+                                       "FP64 gradient summed across ranks on the host in shot "
+                                       "order (gloo)" % dist.world) if dist.world > 1
+                       else "single",
+                       "blocks": blocks},
             "bf16_pml_checkpoints_s_per_shot": res["bf16_pml_checkpoints"]["s_per_shot"],
             "keep_all_s_per_shot": res["keep_all"]["s_per_shot"],
             "keep_all_gradient_identical": keep_same,
