@@ -126,6 +126,13 @@ extern "C" void qp3d_ctx_destroy(qp3d_ctx *ctx)
     adjoint_free(ctx->adj);
     ctx->adj = nullptr;
     if (ctx->errword) cudaFree(ctx->errword);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    for (auto &sl : ctx->sring) {
+        if (sl.dev) cudaFree(sl.dev);
+        if (sl.host) cudaFreeHost(sl.host);
+        if (sl.ready) cudaEventDestroy(sl.ready);
+        if (sl.done) cudaEventDestroy(sl.done);
+    }
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->copy_ev) cudaEventDestroy(ctx->copy_ev);
     for (auto &ev : ctx->ev)
@@ -719,24 +726,36 @@ static int ensure_snap(qp3d_ctx *ctx, size_t n)
     return QP3D_OK;
 }
 
+// The four snapshot regions of the reference (3dPureqPModeling_single_shot.cu:340-377):
+// the interior volume and its mid xz, yz and xy slices.
+struct SnapReq {
+    int kind, x0, x1, y0, y1, z0, z1, n0, n1, n2;
+    size_t size() const { return (size_t)(x1 - x0) * (y1 - y0) * (z1 - z0); }
+};
+
+static void snap_requests(const qp3d_ctx *ctx, SnapReq reqs[4])
+{
+    const int pml = ctx->g.pml, hx = ctx->hx, hy = ctx->hy, hz = ctx->g.nz - 2 * pml;
+    reqs[0] = {QP3D_SNAP_VOLUME, pml, pml + hx, pml, pml + hy, pml, pml + hz, hz, hx, hy};
+    reqs[1] = {QP3D_SNAP_XZ, pml, pml + hx, pml + (hy - 1) / 2, pml + (hy - 1) / 2 + 1, pml, pml + hz,
+               hz, hx, 1};
+    reqs[2] = {QP3D_SNAP_YZ, pml + (hx - 1) / 2, pml + (hx - 1) / 2 + 1, pml, pml + hy, pml, pml + hz,
+               hz, hy, 1};
+    reqs[3] = {QP3D_SNAP_XY, pml, pml + hx, pml, pml + hy, pml + (hz - 1) / 2, pml + (hz - 1) / 2 + 1,
+               hx, hy, 1};
+}
+
 extern "C" int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap)
 {
     if (!ctx || !snap || !snap->fn) return QP3D_ERR_ARG;
     if (!ctx->loaded) return ctx_fail(ctx, QP3D_ERR_STATE, "no shot loaded");
-    const qp3d_geom &g = ctx->g;
-    const int pml = g.pml, hx = ctx->hx, hy = ctx->hy, hz = g.nz - 2 * pml;
     const float *u = ctx->U[ctx->cur];
     const int k = ctx->step - 1;
-    struct Req { int kind, x0, x1, y0, y1, z0, z1, n0, n1, n2; };
-    Req reqs[4] = {
-        {QP3D_SNAP_VOLUME, pml, pml + hx, pml, pml + hy, pml, pml + hz, hz, hx, hy},
-        {QP3D_SNAP_XZ, pml, pml + hx, pml + (hy - 1) / 2, pml + (hy - 1) / 2 + 1, pml, pml + hz, hz, hx, 1},
-        {QP3D_SNAP_YZ, pml + (hx - 1) / 2, pml + (hx - 1) / 2 + 1, pml, pml + hy, pml, pml + hz, hz, hy, 1},
-        {QP3D_SNAP_XY, pml, pml + hx, pml, pml + hy, pml + (hz - 1) / 2, pml + (hz - 1) / 2 + 1, hx, hy, 1},
-    };
-    for (const Req &r : reqs) {
+    SnapReq reqs[4];
+    snap_requests(ctx, reqs);
+    for (const SnapReq &r : reqs) {
         if (!(snap->kinds & (1u << r.kind))) continue;
-        size_t n = (size_t)(r.x1 - r.x0) * (r.y1 - r.y0) * (r.z1 - r.z0);
+        size_t n = r.size();
         int rc = ensure_snap(ctx, n);
         if (rc) return rc;
         CKL(launch_crop(u, ctx->snap_dev, r.x0, r.x1, r.y0, r.y1, r.z0, r.z1, ctx->ldy, ctx->plane,
@@ -748,6 +767,93 @@ extern "C" int qp3d_shot_snapshot(qp3d_ctx *ctx, const qp3d_snap *snap)
         if (snap->fn(snap->user, k, r.kind, ctx->snap_host, r.n0, r.n1, r.n2) != 0)
             return ctx_fail(ctx, QP3D_ERR_CALLBACK, "snapshot callback failed at step %d", k);
     }
+    return QP3D_OK;
+}
+
+// Snapshots of qp3d_forward without stopping the time loop.  A snapshot after
+// step k crops its slices on the step stream into a device slot (the crop
+// runs before step k + 2 overwrites u(k)), and copy_stream moves the slot to
+// its page-locked host twin; the host delivers the slots in step order as
+// their copies land, polling between pieces of steps, and waits only when
+// every slot is taken.  The callbacks therefore see the same data at the same
+// step numbers as with qp3d_shot_snapshot, while later steps already run.
+static int snap_slots(size_t floats)
+{
+    const size_t budget = (size_t)512 << 20;   // bytes of device (and host) slots
+    const size_t n = budget / std::max<size_t>(floats * sizeof(float), 1);
+    return (int)std::max<size_t>(1, std::min<size_t>(n, qp3d_ctx::kSnapSlots));
+}
+
+static int snap_deliver(qp3d_ctx *ctx, const qp3d_snap *snap, int nslots, bool wait)
+{
+    SnapReq reqs[4];
+    snap_requests(ctx, reqs);
+    while (ctx->snap_count > 0) {
+        qp3d_ctx::SnapSlot &sl = ctx->sring[ctx->snap_head];
+        if (!wait) {
+            const cudaError_t q = cudaEventQuery(sl.done);
+            if (q == cudaErrorNotReady) break;
+            CK(q);
+        } else {
+            CK(cudaEventSynchronize(sl.done));
+        }
+        size_t off = 0;
+        for (const SnapReq &r : reqs) {
+            if (!(sl.kinds & (1u << r.kind))) continue;
+            if (snap->fn(snap->user, sl.step, r.kind, sl.host + off, r.n0, r.n1, r.n2) != 0)
+                return ctx_fail(ctx, QP3D_ERR_CALLBACK, "snapshot callback failed at step %d",
+                                sl.step);
+            off += r.size();
+        }
+        ctx->snap_head = (ctx->snap_head + 1) % nslots;
+        --ctx->snap_count;
+    }
+    return QP3D_OK;
+}
+
+static int snap_enqueue(qp3d_ctx *ctx, const qp3d_snap *snap, int nslots)
+{
+    SnapReq reqs[4];
+    snap_requests(ctx, reqs);
+    size_t total = 0;
+    for (const SnapReq &r : reqs)
+        if (snap->kinds & (1u << r.kind)) total += r.size();
+    if (ctx->snap_count == nslots) {
+        // every slot is taken: wait for the oldest, then deliver what has landed
+        CK(cudaEventSynchronize(ctx->sring[ctx->snap_head].done));
+        const int rc = snap_deliver(ctx, snap, nslots, false);
+        if (rc) return rc;
+    }
+    qp3d_ctx::SnapSlot &sl = ctx->sring[(ctx->snap_head + ctx->snap_count) % nslots];
+    if (!sl.ready) {
+        CK(cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+    }
+    if (sl.cap < total) {
+        if (sl.dev) cudaFree(sl.dev);
+        if (sl.host) cudaFreeHost(sl.host);
+        sl.dev = sl.host = nullptr;
+        sl.cap = 0;
+        CK(cudaMalloc(&sl.dev, total * sizeof(float)));
+        CK(cudaMallocHost(&sl.host, total * sizeof(float)));
+        sl.cap = total;
+    }
+    const float *u = ctx->U[ctx->cur];
+    size_t off = 0;
+    for (const SnapReq &r : reqs) {
+        if (!(snap->kinds & (1u << r.kind))) continue;
+        CKL(launch_crop(u, sl.dev + off, r.x0, r.x1, r.y0, r.y1, r.z0, r.z1, ctx->ldy, ctx->plane,
+                        ctx->stream));
+        off += r.size();
+    }
+    CK(cudaEventRecord(sl.ready, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->copy_stream, sl.ready, 0));
+    CK(cudaMemcpyAsync(sl.host, sl.dev, total * sizeof(float), cudaMemcpyDeviceToHost,
+                       ctx->copy_stream));
+    CK(cudaEventRecord(sl.done, ctx->copy_stream));
+    sl.step = ctx->step - 1;
+    sl.kinds = snap->kinds;
+    ++ctx->snap_count;
     return QP3D_OK;
 }
 
@@ -766,12 +872,22 @@ extern "C" int qp3d_forward(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     const bool pinned = cudaPointerGetAttributes(&attr, record) == cudaSuccess &&
                         attr.type == cudaMemoryTypeHost;
     (void)cudaGetLastError();
-    if (pinned && !ctx->copy_stream) {
+    const bool snaps = snap && snap->fn && snap->ntsnap > 0 && snap->kinds;
+    if ((pinned || snaps) && !ctx->copy_stream) {
         CK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ctx->copy_ev, cudaEventDisableTiming));
     }
     const size_t row = (size_t)ctx->hx * ctx->hy;
-    const bool snaps = snap && snap->fn && snap->ntsnap > 0 && snap->kinds;
+    int nslots = 1;
+    if (snaps) {
+        SnapReq reqs[4];
+        snap_requests(ctx, reqs);
+        size_t total = 0;
+        for (const SnapReq &r : reqs)
+            if (snap->kinds & (1u << r.kind)) total += r.size();
+        nslots = snap_slots(total);
+        ctx->snap_head = ctx->snap_count = 0;
+    }
     constexpr int kChunk = 100;   // steps per streamed piece of the record
     int k = 0, sent = 0;
     while (k < g->nt && rc == QP3D_OK) {
@@ -796,9 +912,15 @@ extern "C" int qp3d_forward(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
             }
             sent = k;
         }
-        if (snaps && (k - 1) % snap->ntsnap == 0) rc = qp3d_shot_snapshot(ctx, snap);
+        if (snaps && (k - 1) % snap->ntsnap == 0) rc = snap_enqueue(ctx, snap, nslots);
+        if (snaps && !rc) rc = snap_deliver(ctx, snap, nslots, false);
     }
-    if (!pinned) return rc ? rc : qp3d_shot_read_record(ctx, 0, g->nt, record);
+    if (snaps && !rc) rc = snap_deliver(ctx, snap, nslots, true);
+    if (snaps) ctx->snap_count = 0;   // after an error: the pending slots are dropped
+    if (!pinned) {
+        if (snaps) (void)cudaStreamSynchronize(ctx->copy_stream);
+        return rc ? rc : qp3d_shot_read_record(ctx, 0, g->nt, record);
+    }
     // no copy into the caller's buffer may outlive the call, also on error
     const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
     if (rc) return rc;

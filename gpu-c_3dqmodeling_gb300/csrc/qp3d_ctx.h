@@ -70,10 +70,24 @@ struct qp3d_ctx {
     int step = 0;
     int cur = 0;           // U[cur] holds u(step)
     int prev = 1;          // U[prev] holds u(step-1); the third buffer receives u(step+1)
-    // snapshot staging
+    // snapshot staging (qp3d_shot_snapshot)
     float *snap_dev = nullptr;
     float *snap_host = nullptr;
     size_t snap_cap = 0;
+    // snapshots of qp3d_forward: a ring of slots whose slices are cropped on
+    // the step stream and copied to page-locked memory on copy_stream while
+    // the time loop goes on; the callbacks run in step order once a slot's
+    // copy has landed
+    struct SnapSlot {
+        float *dev = nullptr, *host = nullptr;
+        size_t cap = 0;                       // floats
+        cudaEvent_t ready = nullptr, done = nullptr;
+        int step = -1;
+        unsigned kinds = 0;
+    };
+    static constexpr int kSnapSlots = 4;
+    SnapSlot sring[kSnapSlots];
+    int snap_head = 0, snap_count = 0;        // FIFO of slots waiting for delivery
     cudaEvent_t ev[4] = {};
     cudaEvent_t uev[8] = {};
     // tuning

@@ -1107,6 +1107,9 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
 
     const int x = x0 + r, yq = y0 + 4 * q;
     const bool row_ok = (r < tile_x) && (x < nx - kRadius);
+    // quads wholly in the row padding (y >= ny, the last y tile) neither load
+    // nor store: their cells are not part of the volume
+    const bool mem_ok = row_ok && (yq < ny);
     bool cell_ok[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) cell_ok[j] = row_ok && (yq + j >= kRadius) && (yq + j < ny - kRadius);
@@ -1144,7 +1147,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         const bool pml_quad = xy_face || (row_ok && fz >= 0);
         float4 u1v = zero4, Vv = zero4, Ev = zero4, Rv = zero4;
         uint2 hv = make_uint2(0u, 0u), he = hv, hd = hv;
-        if (row_ok) {
+        if (mem_ok) {
             u1v = ldg4(p.u_prev + base);
             if (HALF) {   // widened after the stencil, when the loads have landed
                 hv = __ldg(reinterpret_cast<const uint2 *>(p.h_vp + base));
@@ -1158,7 +1161,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         }
         float4 w11 = zero4, w12 = zero4, w31 = zero4, w32 = zero4, p1 = zero4, p2 = zero4,
                w21 = zero4;
-        if (pml_quad) {
+        if (pml_quad && mem_ok) {
             w11 = ldg4(p.w1o + base); w12 = ldg4(p.w1c + base);
             w31 = ldg4(p.w3o + base); w32 = ldg4(p.w3c + base);
             p1 = ldg4(p.po + base);   p2 = ldg4(p.pc + base);
@@ -1301,7 +1304,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                     n21[j] = is_pml ? n21[j] : f4(w21, j);
                 }
             }
-            if (pml_quad) {
+            if (pml_quad && mem_ok) {
                 *reinterpret_cast<float4 *>(p.w1n + base) = make_float4(n13[0], n13[1], n13[2], n13[3]);
                 *reinterpret_cast<float4 *>(p.w3n + base) = make_float4(n33[0], n33[1], n33[2], n33[3]);
                 *reinterpret_cast<float4 *>(p.pn + base) = make_float4(n3[0], n3[1], n3[2], n3[3]);
@@ -1334,7 +1337,7 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) out[j] = cell_ok[j] ? out[j] : u0[j];   // never updated
-        if (row_ok) {
+        if (mem_ok) {
             *reinterpret_cast<float4 *>(p.u_out + base) = make_float4(out[0], out[1], out[2], out[3]);
             // receiver plane (3dPureqPModeling_single_shot.cu:333-337)
             if (p.record && z == p.sz && x >= pml && x < nx - pml) {
