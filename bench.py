@@ -550,8 +550,8 @@ def run_batch_arm(args, dist):
     all_shots = synthetic.batch_shots(nshots=args.shots, nt=nt)
     # ranks take contiguous blocks of the shot list, balanced by cells x steps
     blocks = shard.partition([shard.shot_cost(s) for s in all_shots], dist.world)
-    a, b = blocks[dist.rank]
-    shots = all_shots[a:b]
+    blk_a, blk_b = blocks[dist.rank]
+    shots = all_shots[blk_a:blk_b]
     cells = [s.N for s in all_shots]
     work = sum(c * nt for c in cells)
     ctx = qp3d.Context(dist.local)
@@ -823,9 +823,9 @@ def run_adjoint_arm(args, dist):
     # ranks take contiguous blocks of the shots; the FP64 gradient is summed
     # across them in shot order (bit-equal to one process)
     blocks = shard.partition([shard.shot_cost(s) for s in start], dist.world)
-    a, b = blocks[dist.rank]
+    blk_a, blk_b = blocks[dist.rank]
     ctx = qp3d.Context(dist.local)
-    d_obs = {i: ctx.forward(true[i]).copy() for i in range(a, b)}
+    d_obs = {i: ctx.forward(true[i]).copy() for i in range(blk_a, blk_b)}
     res = {}
     gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
@@ -840,8 +840,8 @@ def run_adjoint_arm(args, dist):
                              ("keep_all", 0, 1)):
         ctx.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
         for _ in range(args.warmup):
-            if b > a:
-                ctx.adjoint(start[a], d_obs[a])
+            if blk_b > blk_a:
+                ctx.adjoint(start[blk_a], d_obs[blk_a])
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -857,7 +857,7 @@ def run_adjoint_arm(args, dist):
         cos[p] = round(float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b))), 6)
     keep_same = all(np.array_equal(a, b) for a, b in zip(res["keep_all"]["grads"],
                                                           res["fp32_checkpoints"]["grads"]))
-    ctx.load(start[a] if b > a else start[0])
+    ctx.load(start[blk_a] if blk_b > blk_a else start[0])
     tot, _, _ = ctx.time(nt, per_kernel=False)
     t_fwd = tot / 1e3
     if dist.rank == 0:

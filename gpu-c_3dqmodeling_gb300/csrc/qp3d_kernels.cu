@@ -226,6 +226,10 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
 {
     const int sc = (t + kRadius) % kRing;
     const float *pc = ring + (size_t)sc * slot_floats;
+    // the z taps: planes sc +- (m + 1) of the ring, wrapped by one ring length
+    const float *pcr = pc + rc;
+    const float *pcr_lo = pcr - kRing * (int)slot_floats;
+    const float *pcr_hi = pcr + kRing * (int)slot_floats;
     // y taps: columns c-8 .. c+11 of the centre plane
     float Y[20];
 #pragma unroll
@@ -275,10 +279,9 @@ __device__ __forceinline__ void quad_derivs(const float *ring, size_t slot_float
     float2 gz[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, lz[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
 #pragma unroll
     for (int m = 0; m < kRadius; ++m) {
-        const float *pp = ring + (size_t)slot_add(sc, m + 1) * slot_floats;
-        const float *pm = ring + (size_t)slot_add(sc, -m - 1) * slot_floats;
-        const float4 a = lds4(pp + rc);
-        const float4 b = lds4(pm + rc);
+        const int d = (m + 1) * (int)slot_floats;
+        const float4 a = lds4((sc + m + 1 < kRing ? pcr : pcr_lo) + d);
+        const float4 b = lds4((sc >= m + 1 ? pcr : pcr_hi) - d);
         const float2 a2[2] = {f2(a.x, a.y), f2(a.z, a.w)}, b2[2] = {f2(b.x, b.y), f2(b.z, b.w)};
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
