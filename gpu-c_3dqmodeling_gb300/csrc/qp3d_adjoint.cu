@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 using namespace qp3d;
@@ -232,6 +233,7 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
     a.nx = g->nx; a.ny = g->ny; a.nz = g->nz; a.ldy = ctx->ldy; a.pml = g->pml; a.sz = g->sz;
     a.hx = ctx->hx; a.hy = ctx->hy; a.plane = ctx->plane; a.k = ctx->coefs; a.dt = g->dt;
     a.VP = ctx->VP; a.E2 = ctx->E2; a.R8 = ctx->R8; a.layers = ctx->layers;
+    a.live = ctx->adj_live;
     for (int c = (keep ? 1 : nck) - 1; c >= 0; --c) {
         const int k0 = c * C, k1 = std::min(nt, k0 + C);
         if (!keep) {   // restore the checkpoint, recompute keeping u^k
@@ -285,14 +287,33 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
                              (size_t)ny * 4, (size_t)nx * nz, cudaMemcpyDeviceToHost,
                              ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
-        for (int z = pml; z < nz - pml; ++z)
-            for (int x = pml; x < nx - pml; ++x)
-                for (int y = pml; y < ny - pml; ++y) {
-                    const size_t i = ((size_t)z * nx + x) * ny + y;
-                    double gi = hg[i];
-                    if (q == 0) gi *= 2.0 * (double)m->vp[i] * (double)g->dt * (double)g->dt;
-                    outs[q][i] += gi;
-                }
+        // every cell on its own, so host threads take z slabs
+        double *out = outs[q];
+        auto add = [&](int za, int zb) {
+            for (int z = za; z < zb; ++z)
+                for (int x = pml; x < nx - pml; ++x)
+                    for (int y = pml; y < ny - pml; ++y) {
+                        const size_t i = ((size_t)z * nx + x) * ny + y;
+                        double gi = hg[i];
+                        if (q == 0) gi *= 2.0 * (double)m->vp[i] * (double)g->dt * (double)g->dt;
+                        out[i] += gi;
+                    }
+        };
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nth = (int)std::max(1u, std::min(16u, hw ? hw : 1u));
+        const int hz = nz - 2 * pml;
+        std::vector<std::thread> th;
+        int started = 1;
+        try {
+            for (int t = 1; t < nth; ++t, ++started)
+                th.emplace_back(add, pml + (int)((long long)hz * t / nth),
+                                pml + (int)((long long)hz * (t + 1) / nth));
+        } catch (...) {   // no more threads: this one adds the rest
+        }
+        add(pml, pml + (int)((long long)hz / nth));
+        for (auto &t : th) t.join();
+        for (int t = started; t < nth; ++t)
+            add(pml + (int)((long long)hz * t / nth), pml + (int)((long long)hz * (t + 1) / nth));
     }
     rc = qp3d_shot_sync(ctx);
     if (!rc && misfit) *misfit = J;

@@ -1029,6 +1029,7 @@ extern "C" int qp3d_tune(qp3d_ctx *ctx, const char *key, int value)
     else if (!strcmp(key, "test_hold_plane") && value >= -1) ctx->hold_plane = value + 1;
     else if (!strcmp(key, "adj_ckpt_bf16") && (value == 0 || value == 1)) ctx->adj_bf16 = value;
     else if (!strcmp(key, "adj_keep_all") && value >= -1 && value <= 1) ctx->adj_keep = value;
+    else if (!strcmp(key, "adj_live") && (value == 0 || value == 1)) ctx->adj_live = value;
     else return ctx_fail(ctx, QP3D_ERR_ARG, "unknown tuning key or value: %s=%d", key, value);
     if (ctx->loaded && (!strcmp(key, "tile_x") || !strcmp(key, "chunks"))) {
         CK(cudaSetDevice(ctx->device));
@@ -1057,6 +1058,7 @@ extern "C" int qp3d_tune_get(const qp3d_ctx *ctx, const char *key)
     if (!strcmp(key, "test_hold_plane")) return ctx->hold_plane - 1;
     if (!strcmp(key, "adj_ckpt_bf16")) return ctx->adj_bf16;
     if (!strcmp(key, "adj_keep_all")) return ctx->adj_keep;
+    if (!strcmp(key, "adj_live")) return ctx->adj_live;
     if (!strcmp(key, "batch_graph")) return ctx->batch_graph;
     if (!strcmp(key, "batch_tune")) return ctx->batch_tune;
     if (!strcmp(key, "batch_candidate")) return ctx->batch_candidate;

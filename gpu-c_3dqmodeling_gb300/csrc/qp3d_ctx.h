@@ -125,6 +125,7 @@ struct qp3d_ctx {
     qp3d::AdjState *adj = nullptr;
     int adj_bf16 = 1;                // 1: PML levels of the checkpoints in BF16
     int adj_keep = -1;               // 1: keep every u^k, 0: checkpoints, -1: by free memory
+    int adj_live = 1;                // 1: gradient of the live operator (dS/du included), 0: S frozen
 };
 inline int ctx_fail(qp3d_ctx *c, int code, const char *fmt, ...)
 {

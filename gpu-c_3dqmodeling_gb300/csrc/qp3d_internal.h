@@ -208,6 +208,7 @@ struct AdjParams {
     float *Nu, *Nup, *Nw1, *Nw1o, *Np, *Npo, *Nw21, *Nw3, *Nw3o;
     float *C[6];
     float *gK, *gE, *gD;                   // gradient sums over the steps
+    int live;                              // 1: S's dependence on grad u included
 };
 
 cudaError_t launch_adjoint_step(const AdjParams &a, cudaStream_t stream);

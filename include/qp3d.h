@@ -141,11 +141,14 @@ int qp3d_batch_get_stats(const qp3d_ctx *ctx, qp3d_batch_stats *out);
 
 /* Gradient of the record misfit J = 1/2 sum |record - d_obs|^2 of one shot
  * with respect to vp, epsilon and delta, by the adjoint-state method.  No
- * counterpart in the reference.  The forward is the qp3d_forward step with
- * its scalar operator S frozen per step and cell (threshold decision and
- * unit normal of the forward wavefield; S's dependence on epsilon and delta
- * is differentiated); the adjoint is the exact transpose of that step,
- * split-field PML included.  The backward pass needs u^k of every step: when
+ * counterpart in the reference.  The forward is the qp3d_forward step; the
+ * adjoint is the transpose of its linearization, split-field PML included:
+ * S's dependence on epsilon and delta and (by default, "adj_live" = 1) on
+ * the unit normal of the wavefield gradient are differentiated, so the
+ * result is the gradient of the forward as it runs; only the threshold
+ * decisions (S = 1 below 1% of the step's max |grad u|), which are
+ * discontinuous, are held.  "adj_live" = 0 holds the unit normal as well
+ * (S frozen per step and cell).  The backward pass needs u^k of every step: when
  * all nt wavefields fit in device memory the forward keeps them
  * ("adj_keep_all", default -1: decided by free memory), otherwise it stores
  * checkpoints every ceil(sqrt(nt)) steps and the backward recomputes each
@@ -225,7 +228,8 @@ long long qp3d_ctx_launch_count(const qp3d_ctx *ctx);
  * threshold decisions replayed (default)).
  * "adj_keep_all" (qp3d_adjoint schedule, 1: keep u^k of every step,
  * 0: checkpoints and recomputation, -1: keep all when nt wavefields fit in
- * the free device memory less 8 GiB).
+ * the free device memory less 8 GiB).  "adj_live" (qp3d_adjoint, 1: S's
+ * dependence on grad u included (default), 0: S frozen per step and cell).
  * "arith" (arithmetic of the step, any time): 1 = fast (default: folded
  * 1/h coefficients and fused multiply-adds; within 1e-5 relative L2 of the
  * reference arithmetic over a 1000-step shot), 0 = the reference CPU

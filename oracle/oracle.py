@@ -27,7 +27,7 @@ class OracleArgs(ctypes.Structure):
         ("dlr", _f32p), ("ddlr", _f32p), ("dtb", _f32p), ("ddtb", _f32p),
         ("dfb", _f32p), ("ddfb", _f32p),
         ("c", _f32p), ("c2", _f32p),
-        ("nthreads", ctypes.c_int),
+        ("nthreads", ctypes.c_int), ("live", ctypes.c_int),
     ]
 
 
@@ -312,7 +312,7 @@ class AdjArgs(ctypes.Structure):
         ("dlr", _f32p), ("ddlr", _f32p), ("dtb", _f32p), ("ddtb", _f32p),
         ("dfb", _f32p), ("ddfb", _f32p),
         ("c", _f32p), ("c2", _f32p),
-        ("nthreads", ctypes.c_int),
+        ("nthreads", ctypes.c_int), ("live", ctypes.c_int),
     ]
 
 
@@ -334,13 +334,14 @@ class Adjoint:
     held in double (vp, eps, delta as float64 arrays of N cells) so finite
     differences can perturb it; the scalar operator is frozen by freeze()."""
 
-    def __init__(self, prob, source=True, nthreads=0):
+    def __init__(self, prob, source=True, nthreads=0, live=False):
         self.p = prob
         self.vp = prob.vp.astype(np.float64)
         self.eps = prob.eps.astype(np.float64)
         self.delta = prob.delta.astype(np.float64)
         self.use_source = source
         self.nthreads = nthreads
+        self.live = live          # backward: S's dependence on grad u included
         self.fa = self.fb = None
 
     def _args(self, vp=None, eps=None, delta=None):
@@ -356,6 +357,7 @@ class Adjoint:
         a.dlr, a.ddlr, a.dtb, a.ddtb, a.dfb, a.ddfb = [_fp(x) for x in p.prof]
         a.c, a.c2 = _fp(p.c), _fp(p.c2)
         a.nthreads = self.nthreads
+        a.live = 1 if self.live else 0
         return a
 
     def freeze(self, with_source=True):
@@ -370,6 +372,22 @@ class Adjoint:
         rc = _adj_lib().oracle_adj_freeze(ctypes.byref(a), _ptr(self.fa), _ptr(self.fb))
         assert rc == 0, rc
         return self
+
+    def live_forward(self, vp=None, eps=None, delta=None):
+        """Record of the live operator (S from the run's own wavefield) at the
+        given model: factors frozen on that model, then the run with them."""
+        n = self.p.N * self.p.nt
+        fa = np.zeros(n, np.float64)
+        fb = np.zeros(n, np.float64)
+        a = self._args(vp, eps, delta)
+        rc = _adj_lib().oracle_adj_freeze(ctypes.byref(a), _ptr(fa), _ptr(fb))
+        assert rc == 0, rc
+        keep = self.fa, self.fb
+        self.fa, self.fb = fa, fb
+        try:
+            return self.forward(vp=vp, eps=eps, delta=delta)
+        finally:
+            self.fa, self.fb = keep
 
     def forward(self, extra=None, want_hist=False, vp=None, eps=None, delta=None):
         p = self.p

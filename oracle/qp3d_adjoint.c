@@ -25,6 +25,16 @@
  * term by term.  The gradient is reported on the cells outside the PML shell
  * (the shell's parameters are extensions of the interior edge and are held
  * fixed).
+ *
+ * With live = 1 the backward also differentiates S through the unit normal:
+ * a = (Ux^2 + Uy^2)/s^2 and b = Uz^2/s^2 (s = |grad u| + 2.22e-17) depend on
+ * the first derivatives of u^k, so every cell above the threshold adds
+ * sigma dS/dU_c to the first-derivative fields (c = x, y, z), where sigma is
+ * the adjoint weight of S in the cell's update (lambda K Lap in the
+ * interior; the S-proportional terms of the split-field recursions in the
+ * PML).  That is the gradient of the live forward (S recomputed from the
+ * perturbed wavefield) except for the threshold decisions, which are
+ * discontinuous and held.
  */
 #include "qp3d_oracle.h"
 
@@ -119,6 +129,26 @@ static inline void frozen_s(double a, double b, double e, double dl, double *S, 
         double dS_dq = (a * b != 0.0) ? -0.25 / r : 0.0;
         *dSe = dS_dq * dq_de;
         *dSd = dS_dq * dq_dd;
+    }
+}
+
+/* dS/dUx, dS/dUy, dS/dUz of an above-threshold cell: S of frozen_s through
+ * a = (Ux^2 + Uy^2)/s^2 and b = Uz^2/s^2, s = |grad u| + EPSN (the forms of
+ * step_fwd). */
+static inline void s_grad(const double d[6], double e, double dl, double g[3])
+{
+    double h2 = d[0] * d[0] + d[1] * d[1], v2 = d[2] * d[2];
+    double mode = sqrt(h2 + v2), s = mode + EPSN;
+    double a = h2 / (s * s), b = v2 / (s * s);
+    double D = 1 + 2 * e * a, R8 = 8 * (e - dl);
+    double q = R8 * a * b / (D * D), r = sqrt(1 - q);
+    double dSdq = -0.25 / r;
+    double dqa = R8 * b * (D - 4 * e * a) / (D * D * D), dqb = R8 * a / (D * D);
+    for (int c = 0; c < 3; c++) {
+        double common = d[c] / (mode * s * s * s);
+        double ac = (c < 2 ? 2 * d[c] / (s * s) : 0.0) - 2 * h2 * common;
+        double bc = (c == 2 ? 2 * d[c] / (s * s) : 0.0) - 2 * v2 * common;
+        g[c] = dSdq * (dqa * ac + dqb * bc);
     }
 }
 
@@ -399,6 +429,13 @@ int oracle_adj_backward(const oracle_adj_args *a, const double *fa, const double
                         double d[6];
                         derivs(u, z, x, y, nx, ny, &kc, d);
                         double Lap = e2 * (d[3] + d[4]) + d[5];
+                        if (a->live && (Fa[i] != 0.0 || Fb[i] != 0.0)) {
+                            double gs[3], sig = l * K * Lap;
+                            s_grad(d, e, dl, gs);
+                            C[0][i] += sig * gs[0];
+                            C[1][i] += sig * gs[1];
+                            C[2][i] += sig * gs[2];
+                        }
                         gK[i] += l * S * Lap;
                         ge[i] += l * K * (2 * S * (d[3] + d[4]) + dSe * Lap);
                         gd[i] += l * K * dSd * Lap;
@@ -419,6 +456,19 @@ int oracle_adj_backward(const oracle_adj_args *a, const double *fa, const double
                     if (f <= FR) { C[3][i] += cn; C[0][i] += c1; C[4][i] += ct * e2; C[5][i] += ct; }
                     else if (f <= FBK) { C[4][i] += cn; C[1][i] += c1; C[3][i] += ct * e2; C[5][i] += ct; }
                     else { C[5][i] += cn; C[2][i] += c1; C[3][i] += ct; C[4][i] += ct; }
+                    if (a->live && (Fa[i] != 0.0 || Fb[i] != 0.0)) {
+                        /* the S-proportional terms of w1', p' and w3' */
+                        double d[6], gs[3], Unn, Un, tang;
+                        derivs(u, z, x, y, nx, ny, &kc, d);
+                        if (f <= FR) { Unn = d[3]; Un = d[0]; tang = d[5] + e2 * d[4]; }
+                        else if (f <= FBK) { Unn = d[4]; Un = d[1]; tang = d[5] + e2 * d[3]; }
+                        else { Unn = d[5]; Un = d[2]; tang = d[3] + d[4]; }
+                        double sig = (cn * Unn + c1 * Un + ct * tang) / S;
+                        s_grad(d, e, dl, gs);
+                        C[0][i] += sig * gs[0];
+                        C[1][i] += sig * gs[1];
+                        C[2][i] += sig * gs[2];
+                    }
                 }
         /* transposed stencils: second derivatives symmetric, first antisymmetric */
 #pragma omp parallel for schedule(static)

@@ -114,6 +114,8 @@ typedef struct {
     const float *dlr, *ddlr, *dtb, *ddtb, *dfb, *ddfb;
     const float *c, *c2;
     int nthreads;
+    int live;      /* backward: 1 = also the terms of S's dependence on grad u
+                      (the gradient of the live operator), 0 = S frozen */
 } oracle_adj_args;
 
 /* Base run with the live scalar operator: the frozen factors of every step. */
