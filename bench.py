@@ -47,8 +47,9 @@ steps, sqrt(nt) checkpoints in FP32 (and with BF16 PML levels beside it);
 value = seconds per shot of the gradient (forward, residual, checkpointed
 backward), the records of the true model made first.  Beside it, the schedule
 that keeps every u^k in device memory (88 GB here, no recomputation; the
-library's default when it fits), whose gradient is identical.  Under
-torchrun the shots are split into contiguous blocks across ranks and the FP64
+library's default when it fits), whose gradient is identical.  Two library
+contexts (--adj-contexts) on the GPU run two shots at a time; under torchrun
+the shots are split into contiguous blocks across ranks; either way the FP64
 gradient is summed on the host in shot order, bit-equal to one process
 (shard.py).
 
@@ -105,6 +106,8 @@ def parse():
                     choices=["single", "batch", "large", "adjoint"])
     ap.add_argument("--shots", type=int, default=64,
                     help="batch workload: shots; adjoint workload: up to 16 (a square grid)")
+    ap.add_argument("--adj-contexts", type=int, default=2,
+                    help="adjoint workload: library contexts per GPU running shots at once")
     ap.add_argument("--spec-delta-ppm", type=int, default=None,
                     help="smallest half-width of the predicted max window (ppm)")
     return ap.parse_args()
@@ -684,32 +687,49 @@ def batch_summary(ctx, nshots=64, nt=2000):
                     "records equal the one-call records bit for bit (checked on 4 shots)"}
 
 
+ADJ_CONTEXTS = 2   # library contexts (streams) per GPU running gradient shots at once
+
+
+def gradient_contexts(device, n):
+    import qp3d
+    return [qp3d.Context(device) for _ in range(n)]
+
+
+def timed_gradient(ctxs, start, d_obs, keep):
+    """Gradient of all shots through shard.gradient with one shot per
+    context at a time (the FP64 sum in shot order); (s per shot, J, grads)."""
+    import shard
+    fns = []
+    for c in ctxs:
+        c.tune(adj_keep_all=keep)
+        fns.append(lambda i, s, out, c=c: c.adjoint(s, d_obs[i], out)[0])
+    for c in ctxs:   # first call of each context: buffers and schedule
+        c.adjoint(start[0], d_obs[0])
+    t0 = time.perf_counter()
+    J, grads = shard.gradient(start, fns if len(fns) > 1 else fns[0],
+                              group=shard.Group())
+    return (time.perf_counter() - t0) / len(start), J, grads
+
+
 def adjoint_summary(ctx, grid=4, nt=2000):
     """Misfit gradient of the 16-shot gradient workload with the library's
     default schedule (every u^k kept when they fit in device memory), and
     with the sqrt(nt) checkpoint schedule in its default storage (BF16 PML
     levels, the forward's threshold decisions replayed), beside the forward
     alone of the same shots; the checkpointed gradient's cosine against the
-    kept one (FP32 checkpoints give the kept gradient bit for bit)."""
+    kept one (FP32 checkpoints give the kept gradient bit for bit).  Two
+    library contexts run two shots at a time (the adjoint passes are
+    latency-bound: one context per GPU measured 1.23 s per shot, two 1.07)."""
     import synthetic
     true, start = synthetic.adjoint_case(nt=nt, grid=grid)
     d_obs = [ctx.forward(s).copy() for s in true]
-    N = start[0].N
-
-    def run(keep):
-        ctx.tune(adj_keep_all=keep)
-        grads = [np.zeros(N, np.float64) for _ in range(3)]
-        ctx.adjoint(start[0], d_obs[0])
-        t0 = time.perf_counter()
-        J = 0.0
-        for s, d in zip(start, d_obs):
-            j, _ = ctx.adjoint(s, d, grads)
-            J += j
-        return (time.perf_counter() - t0) / len(start), J, grads
-
-    sec, J, g_keep = run(-1)
-    sec_ck, J_ck, g_ck = run(0)
-    ctx.tune(adj_keep_all=-1)
+    ctxs = gradient_contexts(ctx.device, ADJ_CONTEXTS)
+    try:
+        sec, J, g_keep = timed_gradient(ctxs, start, d_obs, -1)
+        sec_ck, J_ck, g_ck = timed_gradient(ctxs, start, d_obs, 0)
+    finally:
+        for c in ctxs:
+            c.close()
     cos = [float(np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b)))
            for a, b in zip(g_ck, g_keep)]
     ctx.load(start[0])
@@ -717,7 +737,8 @@ def adjoint_summary(ctx, grid=4, nt=2000):
     return {"metric": "adjoint grad s/shot", "value": round(sec, 4), "unit": "s/shot",
             "higher_is_better": False, "workload": ADJ_NAME % (len(start), nt),
             "forward_only_s_per_shot": round(t_fwd, 4),
-            "schedule": "default (every u^k kept when nt wavefields fit in device memory)",
+            "schedule": "default (every u^k kept when nt wavefields fit in device memory); "
+                        "%d library contexts on the GPU, one shot each at a time" % ADJ_CONTEXTS,
             "misfit": J,
             "checkpointed": {"s_per_shot": round(sec_ck, 4), "misfit": J_ck,
                              "schedule": "ceil(sqrt(nt)) checkpoints, PML levels in BF16, "
@@ -834,27 +855,31 @@ def run_adjoint_arm(args, dist):
     gpu_index = (os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[dist.local]
                  if os.environ.get("CUDA_VISIBLE_DEVICES") else dist.local)
 
-    def one_shot(i, s, out):
-        J, _ = ctx.adjoint(s, d_obs[i], out)
-        return J
+    # contexts (streams) on this rank's GPU running gradient shots at once
+    ctxs = [ctx] + gradient_contexts(dist.local, max(1, args.adj_contexts) - 1)
+    fns = [lambda i, s, out, c=c: c.adjoint(s, d_obs[i], out)[0] for c in ctxs]
 
     clocks = Clocks(gpu_index)
-    launches0 = ctx.launch_count()
+    launches0 = sum(c.launch_count() for c in ctxs)
     for name, bf16, keep in (("fp32_checkpoints", 0, 0), ("bf16_pml_checkpoints", 1, 0),
                              ("keep_all", 0, 1)):
-        ctx.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
+        for c in ctxs:
+            c.tune(adj_ckpt_bf16=bf16, adj_keep_all=keep)
         for _ in range(args.warmup):
             if blk_b > blk_a:
-                ctx.adjoint(start[blk_a], d_obs[blk_a])
+                for c in ctxs:
+                    c.adjoint(start[blk_a], d_obs[blk_a])
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            J, grads = shard.gradient(start, one_shot)
+            J, grads = shard.gradient(start, fns if len(fns) > 1 else fns[0])
         sec = dist.max(time.perf_counter() - t0)
         res[name] = {"s_per_shot": round(sec / (args.steps * len(start)), 4),
                      "misfit": J, "grads": grads}
     clk = clocks.stop()
-    gpu_launches = ctx.launch_count() - launches0
+    gpu_launches = sum(c.launch_count() for c in ctxs) - launches0
+    for c in ctxs[1:]:
+        c.close()
     cos = {}
     for i, p in enumerate(("vp", "eps", "delta")):
         a, b = res["bf16_pml_checkpoints"]["grads"][i], res["fp32_checkpoints"]["grads"][i]
@@ -879,6 +904,7 @@ def run_adjoint_arm(args, dist):
                                        "FP64 gradient summed across ranks on the host in shot "
                                        "order (gloo)" % dist.world) if dist.world > 1
                        else "single",
+                       "contexts_per_gpu": len(ctxs),
                        "blocks": blocks},
             "bf16_pml_checkpoints_s_per_shot": res["bf16_pml_checkpoints"]["s_per_shot"],
             "keep_all_s_per_shot": res["keep_all"]["s_per_shot"],

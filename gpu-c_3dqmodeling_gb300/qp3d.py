@@ -337,6 +337,7 @@ class Context:
         if rc != QP3D_OK:
             raise QP3DError("qp3d_ctx_create(%d) failed: %s" % (device, ERRORS.get(rc, rc)))
         self.h = h
+        self.device = device
         self._shot = None
 
     def close(self):

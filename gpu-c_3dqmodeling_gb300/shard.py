@@ -139,27 +139,79 @@ def gradient(shots, grad_fn, group=None, costs=None, n=None):
     returns its misfit.  Each rank calls it for its own block only: rank 0
     passes its running sums (it starts from zero, as one process does), the
     other ranks a zeroed set per shot (0 + t equals t exactly), whose terms
-    they add to the running sum of the lower ranks once it arrives.  n: cells
-    per array (default shots[0].N).  Returns (J, [G_vp, G_eps, G_delta]) on
-    every rank, equal bit for bit to one process calling grad_fn for every
-    shot in shot order on one set of zeroed arrays."""
+    they add to the running sum of the lower ranks once it arrives.  A list
+    of such functions (one per library context, each with its own stream on
+    the rank's GPU) runs that many shots of the block at once on host
+    threads; their terms land in zeroed arrays and are added in shot order.
+    n: cells per array (default shots[0].N).  Returns (J, [G_vp, G_eps,
+    G_delta]) on every rank, equal bit for bit to one process calling
+    grad_fn for every shot in shot order on one set of zeroed arrays."""
     group = group or Group.from_torch()
     costs = [shot_cost(s) for s in shots] if costs is None else costs
     a, b = my_block(costs, group.rank, group.world)
     n = shots[0].N if n is None else n
-    if group.rank == 0:
+    fns = list(grad_fn) if isinstance(grad_fn, (list, tuple)) else [grad_fn]
+    Js, gs = [], [[], [], []]
+
+    def keep(J, out):
+        if group.rank == 0:
+            if not Js:
+                Js.append(0.0)
+                for q in range(3):
+                    gs[q].append(np.zeros(n, np.float64))
+            Js[0] += J
+            for q in range(3):
+                gs[q][0] += out[q]
+        else:
+            Js.append(J)
+            for q in range(3):
+                gs[q].append(out[q])
+
+    if len(fns) == 1 and group.rank == 0:
         acc = [np.zeros(n, np.float64) for _ in range(3)]
         J0 = 0.0
         for i in range(a, b):
-            J0 += grad_fn(i, shots[i], acc)
+            J0 += fns[0](i, shots[i], acc)
         Js, gs = [J0], [[acc[q]] for q in range(3)]
-    else:
-        Js, gs = [], [[], [], []]
+    elif len(fns) == 1:
         for i in range(a, b):
             out = [np.zeros(n, np.float64) for _ in range(3)]
-            Js.append(grad_fn(i, shots[i], out))
-            for q in range(3):
-                gs[q].append(out[q])
+            keep(fns[0](i, shots[i], out), out)
+    else:
+        import queue
+        from collections import deque
+        from concurrent.futures import ThreadPoolExecutor
+        free = queue.Queue()
+        for f in fns:
+            free.put(f)
+
+        def task(i, out):
+            for t in out:      # recycled arrays: zeroed in place
+                t.fill(0.0)
+            f = free.get()
+            try:
+                return f(i, shots[i], out), out
+            finally:
+                free.put(f)
+
+        # at most one shot more in flight than there are contexts; the main
+        # thread adds the terms in shot order and recycles rank 0's arrays
+        pending, spare = deque(), []
+
+        def consume():
+            J, out = pending.popleft().result()
+            keep(J, out)
+            if group.rank == 0:
+                spare.append(out)
+
+        with ThreadPoolExecutor(len(fns)) as ex:
+            for i in range(a, b):
+                if len(pending) > len(fns):
+                    consume()
+                out = spare.pop() if spare else [np.empty(n, np.float64) for _ in range(3)]
+                pending.append(ex.submit(task, i, out))
+            while pending:
+                consume()
     J = float(ordered_sum([np.array([v]) for v in Js], group, 1)[0])
     G = [ordered_sum(gs[q], group, n) for q in range(3)]
     return J, G

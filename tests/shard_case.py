@@ -75,9 +75,10 @@ def worker(rank, world, port, kind, out_q):
     dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank,
                             world_size=world)
     try:
-        if kind == "fake":
+        if kind in ("fake", "fake2"):
             shots = [FakeShot(i) for i in range(7)]
-            J, G = shard.gradient(shots, adding(lambda i, s: fake_terms(i)))
+            fn = adding(lambda i, s: fake_terms(i))
+            J, G = shard.gradient(shots, [fn, fn, fn] if kind == "fake2" else fn)
             blk, recs = shard.records(shots, lambda b: [fake_record(s) for s in b])
         else:
             shots = oracle_shots()

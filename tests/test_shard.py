@@ -92,8 +92,8 @@ def _one_process(shots, fn):
     return J, G
 
 
-@pytest.mark.parametrize("world", [2, 3])
-def test_gradient_sum_bit_equal_to_one_process(world):
+@pytest.mark.parametrize("world,kind", [(2, "fake"), (3, "fake"), (2, "fake2")])
+def test_gradient_sum_bit_equal_to_one_process(world, kind):
     shots = [shard_case.FakeShot(i) for i in range(7)]
     J1, G1 = _one_process(shots, lambda i, s: shard_case.fake_terms(i))
     # the stand-in terms do depend on the order of the additions
@@ -101,7 +101,7 @@ def test_gradient_sum_bit_equal_to_one_process(world):
     for i in reversed(range(7)):
         rev += shard_case.fake_terms(i)[1][0]
     assert not np.array_equal(rev, G1[0])
-    out = _run(world, "fake")
+    out = _run(world, kind)
     for rank in range(world):
         J, G, blk, recs = out[rank]
         assert J == J1
@@ -131,3 +131,26 @@ def test_oracle_gradient_across_two_ranks():
         assert J == J1
         for q in range(3):
             assert np.array_equal(G[q].view(np.uint64), G1[q].view(np.uint64))
+
+
+def test_concurrent_contexts_in_one_process():
+    """Several grad functions (library contexts on one GPU) run shots at once;
+    the terms are still added in shot order: the same bits as one function."""
+    import threading
+    shots = [shard_case.FakeShot(i) for i in range(9)]
+    J1, G1 = _one_process(shots, lambda i, s: shard_case.fake_terms(i))
+    lock = threading.Lock()
+    busy = []
+
+    def fn(i, s, out):
+        with lock:
+            busy.append(i)
+        J, g = shard_case.fake_terms(i)
+        for q in range(3):
+            out[q] += g[q]
+        return J
+
+    J, G = shard.gradient(shots, [fn, fn, fn], group=shard.Group())
+    assert J == J1 and sorted(busy) == list(range(9))
+    for q in range(3):
+        assert np.array_equal(G[q].view(np.uint64), G1[q].view(np.uint64))
