@@ -167,3 +167,34 @@ def test_bf16_checkpoints_at_reduced_gradient_workload():
         c = _cos(a, b)
         print("reduced gradient workload, BF16 PML checkpoints %s: cosine %.6f" % (name, c))
         assert c >= 0.999, (name, c)
+
+
+def test_gradient_on_two_contexts_equals_one():
+    """shard.gradient with two library contexts on the GPU (two shots at a
+    time, each on its own stream and host thread) adds the shots' terms in
+    shot order: bit for bit the gradient of one context taking the shots in
+    turn, keeping every u^k and with BF16 checkpoints."""
+    import shard
+    shots, d_obs = [], []
+    with qp3d.Context(0) as ctx:
+        for seed in (51, 52, 53, 54):
+            s = synthetic.small_case(hx=22, hy=20, nz0=18, pml=8, nt=80, seed=seed, fm=30.0)
+            true = qp3d.Shot(s.nx, s.ny, s.nz, s.pml, s.sz, s.dx, s.dy, s.dz, s.dt,
+                             (s.vp * np.float32(1.02)).astype(np.float32), s.eps, s.delta, s.src,
+                             s.wavelet, s.prof, s.c, s.c2)
+            shots.append(s)
+            d_obs.append(ctx.forward(true).copy())
+    N = shots[0].N
+    for keep in (1, 0):
+        with qp3d.Context(0) as c0, qp3d.Context(0) as c1:
+            for c in (c0, c1):
+                c.tune(adj_keep_all=keep)
+            one = [np.zeros(N, np.float64) for _ in range(3)]
+            J1 = 0.0
+            for s, d in zip(shots, d_obs):
+                J1 += c0.adjoint(s, d, one)[0]
+            fns = [lambda i, s, out, c=c: c.adjoint(s, d_obs[i], out)[0] for c in (c0, c1)]
+            J2, two = shard.gradient(shots, fns, group=shard.Group())
+        assert J2 == pytest.approx(J1, rel=1e-12)
+        for a, b in zip(one, two):
+            assert np.array_equal(a.view(np.uint64), b.view(np.uint64))

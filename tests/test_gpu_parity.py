@@ -312,3 +312,59 @@ def test_pinned_record_is_streamed_identically(ctx):
             assert bits_equal(pin.array, want)
         finally:
             pin.free()
+
+
+def test_snapshot_ring_order_and_failure(ctx):
+    """qp3d_forward hands snapshots over from a ring of device / page-locked
+    slots while later steps already run: every snapshot arrives, in step
+    order, equal to the staged path's (qp3d_shot_snapshot after the same
+    step), also when the ring wraps many times and with a page-locked record;
+    a callback that fails stops the call with QP3D_ERR_CALLBACK at its own
+    step and leaves the context usable."""
+    shot = synthetic.small_case(hx=20, hy=18, nz0=16, pml=6, nt=120, seed=9)
+    kinds = [qp3d.SNAP_VOLUME, qp3d.SNAP_XZ, qp3d.SNAP_YZ]
+    every = 7
+    want_steps = [k for k in range(shot.nt) if k % every == 0]
+
+    def collect(into):
+        def cb(step, kind, arr):
+            into.append((step, kind, arr))
+            return 0
+        return qp3d.make_snap(cb, every, kinds)
+
+    got = []
+    rec = ctx.forward(shot, snap=collect(got))
+    pin = qp3d.PinnedArray(rec.shape)
+    got_pinned = []
+    try:
+        ctx.forward(shot, snap=collect(got_pinned), record=pin.array)
+        assert bits_equal(pin.array, rec)
+    finally:
+        pin.free()
+    ref = []
+    snap_ref = collect(ref)
+    ctx.load(shot)
+    k = 0
+    while k < shot.nt:
+        nxt = k if k % every == 0 else (k // every + 1) * every
+        n = min(shot.nt - k, nxt - k + 1)
+        ctx.advance(n)
+        k += n
+        if (k - 1) % every == 0:
+            ctx.snapshot(snap_ref)
+    assert [s for s, _, _ in ref] == sorted(s for s, _, _ in ref)
+    assert sorted({s for s, _, _ in ref}) == want_steps
+    for run in (got, got_pinned):
+        assert len(run) == len(ref) == len(want_steps) * len(kinds)
+        for (s1, k1, a1), (s2, k2, a2) in zip(run, ref):
+            assert s1 == s2 and k1 == k2 and bits_equal(a1, a2)
+    seen = []
+
+    def bad(step, kind, arr):
+        seen.append(step)
+        return 1 if step >= 21 else 0
+
+    with pytest.raises(qp3d.QP3DError, match=r"\(-7 "):
+        ctx.forward(shot, snap=qp3d.make_snap(bad, every, [qp3d.SNAP_XZ]))
+    assert seen == [0, 7, 14, 21]
+    assert bits_equal(ctx.forward(shot), rec)
