@@ -1959,18 +1959,18 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
         const float4 Kv = make_float4(k_of_vp(Vv.x, a.dt), k_of_vp(Vv.y, a.dt),
                                       k_of_vp(Vv.z, a.dt), k_of_vp(Vv.w, a.dt));
         const float T2 = *a.T2;
-        // wa: with the live operator, dS/da times 2 / m2^2, so that the
-        // derivatives of S in Ux, Uy, Uz are wa (Ux Uz^2, Uy Uz^2, -Uz h2)
-        // (a = h2 / m2 = nx^2 + ny^2, h2 = Ux^2 + Uy^2, m2 = h2 + Uz^2)
-        float KS[4], e2[4], S[4], dSe[4], dSd[4], wa[4], h2v[4];
+        // wa: with the live operator, dS/da times 2 / m2, so that the
+        // derivatives of S in Ux, Uy, Uz are wa (Ux (1 - a), Uy (1 - a), -Uz a)
+        // (a = h2 / m2 = nx^2 + ny^2, h2 = Ux^2 + Uy^2, m2 = h2 + Uz^2; no
+        // power of m2 above the first, which could leave the float range)
+        float KS[4], e2[4], S[4], dSe[4], dSd[4], wa[4], av[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const float E2 = f4(Ev, j), R8 = f4(Rv, j);
             e2[j] = 1.0f + E2;
             const float h2 = fmaf(Uy[j], Uy[j], Ux[j] * Ux[j]), m2 = fmaf(Uz[j], Uz[j], h2);
-            h2v[j] = h2;
             S[j] = 1.0f;
-            dSe[j] = dSd[j] = wa[j] = 0.0f;
+            dSe[j] = dSd[j] = wa[j] = av[j] = 0.0f;
             const bool on = a.dec ? ((a.dec[i >> 5] >> ((unsigned)(i & 31) + j)) & 1u) != 0
                                   : (m2 > T2);
             if (on) {
@@ -1985,7 +1985,8 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
                 dSd[j] = -dSdq * ab8;
                 if (a.live) {   // dq/da = R8 ((1 - 2a) D - 2 E2 a (1 - a)) / D^3
                     const float dqda = R8 * ((1.0f - 2.0f * aa) * D - 2.0f * E2 * aa * bb) * iD * iD * iD;
-                    wa[j] = dSdq * dqda * __fdividef(2.0f, m2 * m2);
+                    wa[j] = __fdividef(2.0f * dSdq * dqda, m2);
+                    av[j] = aa;
                 }
             }
             KS[j] = f4(Kv, j) * S[j];
@@ -2010,10 +2011,10 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
                 gD[j] += l[j] * Kc * dSd[j] * Lap;
                 // live operator: S's dependence on grad u, through the
                 // transposed first derivatives (zero where S = 1)
-                const float w = l[j] * Kc * Lap * wa[j], v2 = Uz[j] * Uz[j];
-                c0[j] = w * Ux[j] * v2;
-                c1[j] = w * Uy[j] * v2;
-                c2[j] = -w * Uz[j] * h2v[j];
+                const float w = l[j] * Kc * Lap * wa[j], bv = 1.0f - av[j];
+                c0[j] = w * Ux[j] * bv;
+                c1[j] = w * Uy[j] * bv;
+                c2[j] = -w * Uz[j] * av[j];
             }
             QP3D_ST4(a.gK, gK); QP3D_ST4(a.gE, gE); QP3D_ST4(a.gD, gD); QP3D_ST4(a.Nup, nup);
         }
@@ -2052,10 +2053,10 @@ __global__ void __launch_bounds__(256, 2) qp3d_adj_a_kernel(const AdjParams a)
                     const float tang = isz ? Uxx[j] + Uyy[j]
                                            : fmaf(e2[j], f[j] < 2 ? Uyy[j] : Uxx[j], Uzz[j]);
                     const float w = __fdividef(cn * Unn + cf * Un + ct * tang, S[j]) * wa[j];
-                    const float v2 = Uz[j] * Uz[j];
-                    c0[j] += w * Ux[j] * v2;
-                    c1[j] += w * Uy[j] * v2;
-                    c2[j] -= w * Uz[j] * h2v[j];
+                    const float bv = 1.0f - av[j];
+                    c0[j] += w * Ux[j] * bv;
+                    c1[j] += w * Uy[j] * bv;
+                    c2[j] -= w * Uz[j] * av[j];
                 }
             }
             QP3D_ST4(a.Nw1, nw1); QP3D_ST4(a.Nw1o, nw1o); QP3D_ST4(a.Np, np_);
