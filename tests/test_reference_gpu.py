@@ -6,8 +6,9 @@ The reference kernels are driven in the reference GPU driver's step sequence
 the same scheme as CPU_function.c but with nvcc's default contraction of a*b+c
 into fused multiply-adds and double-precision literals in scalar_operator
 (GPU_kernel.cu:87-115), so they are not bit-identical to the CPU operators;
-every figure below is printed, and the bounds are the spec ones where
-they hold for the reference's own two implementations.
+every figure below is printed, and the bounds are the parity bounds of the
+path (relative L2 <= 1e-5, max abs <= 1e-4 of the peak) where they hold for
+the reference's own two implementations.
 """
 import numpy as np
 import pytest
