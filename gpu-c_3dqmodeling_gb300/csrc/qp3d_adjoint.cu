@@ -44,6 +44,8 @@ using namespace qp3d;
 // qp3d_api.cu
 int qp3d_internal_enqueue_step(qp3d_ctx *ctx);
 int qp3d_internal_restore_step(qp3d_ctx *ctx, int step);
+int qp3d_internal_bind_wavefields(qp3d_ctx *ctx, float *u_prev, float *u_cur, float *u_next);
+int qp3d_internal_restore_wavefields(qp3d_ctx *ctx, float *const U[3]);
 
 namespace qp3d {
 
@@ -104,6 +106,8 @@ int alloc_state(qp3d_ctx *ctx, AdjState *s, int C, int nck, int bf16, int keep, 
     for (auto *&p : s->Cf) CK(cudaMalloc(&p, vb));
     for (auto *&p : s->g) CK(cudaMalloc(&p, vb));
     CK(cudaMalloc(&s->seg, vb * C));
+    // the row padding of a wavefield is never written by a step: zero it once
+    CK(cudaMemset(s->seg, 0, vb * C));
     const size_t per = (size_t)s->vol * (bf16 ? 2 * sizeof(float) + 7 * sizeof(__nv_bfloat16)
                                               : 9 * sizeof(float));
     if (nck) CK(cudaMalloc(&s->ck, per * nck));
@@ -194,11 +198,25 @@ extern "C" int qp3d_adjoint(qp3d_ctx *ctx, const qp3d_geom *g, const qp3d_model 
         ctx->dec_words = vol / 32;
         ctx->dec_mode = 1;
     }
-    // ---- forward, keeping u^k or checkpoints
+    // ---- forward, keeping u^k or checkpoints.  Keeping every u^k, the steps
+    // write u(k+1) straight into its slot of the kept array (no copy per
+    // step); the shot's own buffers serve as u(-1) (zero after the reset) and
+    // receive u(nt), and are put back afterwards, also on an error.
+    float *const own[3] = {ctx->U[0], ctx->U[1], ctx->U[2]};
+    struct OwnGuard {
+        qp3d_ctx *c;
+        float *const *u;
+        bool on;
+        ~OwnGuard() { if (on) (void)qp3d_internal_restore_wavefields(c, u); }
+    } own_guard{ctx, own, keep != 0};
+    if (keep) CK(cudaMemsetAsync(S->seg, 0, vb, ctx->stream));   // u^0
     for (int k = 0; k < nt; ++k) {
         if (keep) {
-            CK(cudaMemcpyAsync(S->seg + (size_t)k * vol, ctx->U[ctx->cur], vb,
-                               cudaMemcpyDeviceToDevice, ctx->stream));
+            float *u_prev = k ? S->seg + (size_t)(k - 1) * vol : ctx->U[ctx->prev];
+            float *u_next = k + 1 < nt ? S->seg + (size_t)(k + 1) * vol : own[3 - ctx->cur - ctx->prev];
+            if (k == 0) u_prev = own[ctx->prev];
+            if ((rc = qp3d_internal_bind_wavefields(ctx, u_prev, S->seg + (size_t)k * vol, u_next)))
+                return rc;
         } else if (k % C == 0) {
             float *v[9];
             live_state(ctx, k, v);

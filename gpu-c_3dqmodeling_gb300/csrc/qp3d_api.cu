@@ -492,6 +492,31 @@ int qp3d_internal_enqueue_step(qp3d_ctx *ctx)
     return enqueue_step(ctx, nullptr, nullptr, nullptr, nullptr);
 }
 
+// Wavefield buffers chosen by the caller for the next step (qp3d_adjoint keeps
+// every u^k in an array of its own): the step reads u(k-1) from u_prev and
+// u(k) from u_cur (its TMA map is encoded for that buffer) and writes u(k+1)
+// to u_next.  Launches already enqueued keep the maps they were given.
+int qp3d_internal_bind_wavefields(qp3d_ctx *ctx, float *u_prev, float *u_cur, float *u_next)
+{
+    const int a = ctx->cur, b = ctx->prev, c = 3 - a - b;
+    ctx->U[a] = u_cur;
+    ctx->U[b] = u_prev;
+    ctx->U[c] = u_next;
+    return make_tmap(ctx, u_cur, &ctx->tm[a]);
+}
+
+// The shot's own three wavefield buffers back in place, with their maps.
+int qp3d_internal_restore_wavefields(qp3d_ctx *ctx, float *const U[3])
+{
+    int rc = QP3D_OK;
+    for (int i = 0; i < 3; ++i) {
+        ctx->U[i] = U[i];
+        const int r = make_tmap(ctx, U[i], &ctx->tm[i]);
+        if (r && !rc) rc = r;
+    }
+    return rc;
+}
+
 int qp3d_internal_restore_step(qp3d_ctx *ctx, int step)
 {
     if (step < 0 || step >= ctx->g.nt) return ctx_fail(ctx, QP3D_ERR_ARG, "bad step %d", step);
