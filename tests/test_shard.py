@@ -154,3 +154,19 @@ def test_concurrent_contexts_in_one_process():
     assert J == J1 and sorted(busy) == list(range(9))
     for q in range(3):
         assert np.array_equal(G[q].view(np.uint64), G1[q].view(np.uint64))
+
+
+def test_partition_of_the_batched_workload_is_balanced():
+    """The 64 uneven shots of the batched workload (padded cells x steps):
+    for 2 to 8 ranks the largest block exceeds the mean by at most one
+    shot's cost, and the blocks cover the list in order."""
+    import synthetic
+    pml, nt = 20, 2000
+    costs = [float((hx + 2 * pml) * (hy + 2 * pml) * (nz0 + 2 * pml) * nt)
+             for _, _, hx, hy, nz0, _ in synthetic.batch_windows(64)]
+    for world in range(2, 9):
+        blocks = shard.partition(costs, world)
+        assert blocks[0][0] == 0 and blocks[-1][1] == 64
+        loads = [sum(costs[a:b]) for a, b in blocks]
+        assert max(loads) <= sum(costs) / world + max(costs), (world, loads)
+        print("%d ranks: largest block %.3f x the mean" % (world, max(loads) * world / sum(costs)))
