@@ -323,7 +323,9 @@ def _adj_lib():
         L.oracle_adj_freeze.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_adj_forward.argtypes = [P] + [ctypes.c_void_p] * 5
         L.oracle_adj_backward.argtypes = [P] + [ctypes.c_void_p] * 8
-        for f in (L.oracle_adj_freeze, L.oracle_adj_forward, L.oracle_adj_backward):
+        L.oracle_adj_tlm.argtypes = [P] + [ctypes.c_void_p] * 5
+        for f in (L.oracle_adj_freeze, L.oracle_adj_forward, L.oracle_adj_backward,
+                  L.oracle_adj_tlm):
             f.restype = ctypes.c_int
         L._adj_ready = True
     return L
@@ -399,6 +401,19 @@ class Adjoint:
                                            _ptr(ex), _ptr(rec), _ptr(hist))
         assert rc == 0, rc
         return (rec, hist) if want_hist else rec
+
+    def tlm(self, hist, extra):
+        """Records of the tangent-linear response to additive sources extra
+        (nt x N) about the base trajectory hist (from forward(want_hist=True));
+        with live, S's perturbation through the unit normal is included."""
+        p = self.p
+        rec = np.zeros((p.nt, p.nx - 2 * p.pml, p.ny - 2 * p.pml), np.float64)
+        a = self._args()
+        ex = np.ascontiguousarray(extra, np.float64).ravel()
+        rc = _adj_lib().oracle_adj_tlm(ctypes.byref(a), _ptr(self.fa), _ptr(self.fb),
+                                       _ptr(hist), _ptr(ex), _ptr(rec))
+        assert rc == 0, rc
+        return rec
 
     def backward(self, hist, resid, want_fadj=False):
         p = self.p

@@ -365,6 +365,107 @@ out:
     return rc;
 }
 
+/* One tangent-linear step about the base wavefield ub = u^k: the frozen step
+ * of the perturbation s (no source: it does not depend on the state) plus,
+ * with live, the perturbation of S through the unit normal, dS = sum_c
+ * dS/dU_c (base) D_c du, times the S-proportional terms of the base update. */
+static void tlm_step(const oracle_adj_args *a, const dcoef *kc, const state *s, state *n,
+                     const double *fa, const double *fb, const double *ub, const double *extra)
+{
+    int nx = a->nx, ny = a->ny, nz = a->nz, pml = a->pml;
+    double dt = a->dt;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < nz; z++)
+        for (int x = 0; x < nx; x++)
+            for (int y = 0; y < ny; y++) {
+                size_t i = IX(z, x, y);
+                double un;
+                n->w1[i] = n->w1o[i] = n->p[i] = n->po[i] = 0;
+                n->w21[i] = n->w3[i] = n->w3o[i] = 0;
+                if (!updated(z, x, y, nx, ny, nz)) {
+                    un = s->u[i];
+                } else {
+                    double d[6], db[6], gs[3], dS = 0.0;
+                    derivs(s->u, z, x, y, nx, ny, kc, d);
+                    derivs(ub, z, x, y, nx, ny, kc, db);
+                    double e = a->eps[i], dl = a->del[i], v = a->vp[i], S;
+                    frozen_s(fa[i], fb[i], e, dl, &S, NULL, NULL);
+                    int live_on = a->live && (fa[i] != 0.0 || fb[i] != 0.0);
+                    if (live_on) {
+                        s_grad(db, e, dl, gs);
+                        dS = gs[0] * d[0] + gs[1] * d[1] + gs[2] * d[2];
+                    }
+                    int f = region_a(z, x, y, nx, ny, nz, pml);
+                    double e2 = 1 + 2 * e;
+                    if (f < 0) {
+                        double K = (v * dt) * (v * dt);
+                        un = 2 * s->u[i] - s->up[i] + K * S * (e2 * (d[3] + d[4]) + d[5]);
+                        if (live_on) un += K * (e2 * (db[3] + db[4]) + db[5]) * dS;
+                    } else {
+                        pml_coef c;
+                        pml_cell_coef(a, f, layer_a(f, z, x, y, nx, ny, nz, pml), S, e, v, &c);
+                        double Unn, Un, tang, Unb, Ub, tb;
+                        if (f <= FR) {
+                            Unn = d[3]; Un = d[0]; tang = d[5] + e2 * d[4];
+                            Unb = db[3]; Ub = db[0]; tb = db[5] + e2 * db[4];
+                        } else if (f <= FBK) {
+                            Unn = d[4]; Un = d[1]; tang = d[5] + e2 * d[3];
+                            Unb = db[4]; Ub = db[1]; tb = db[5] + e2 * db[3];
+                        } else {
+                            Unn = d[5]; Un = d[2]; tang = d[3] + d[4];
+                            Unb = db[5]; Ub = db[2]; tb = db[3] + db[4];
+                        }
+                        double w1n = c.A * Unn - c.a1 * s->w1[i] + c.a2 * s->w1o[i];
+                        double pn = -c.a1 * s->p[i] + c.a2 * s->po[i] + c.sgn * c.A * c.dd * Un;
+                        double w3n = c.At * tang + 2 * s->w3[i] - s->w3o[i];
+                        if (live_on) {   /* A and At are proportional to S */
+                            w1n += c.A / S * Unb * dS;
+                            pn += c.sgn * c.A / S * c.dd * Ub * dS;
+                            w3n += c.At / S * tb * dS;
+                        }
+                        double w21n = dt * pn + c.a3 * s->w21[i];
+                        n->w1[i] = w1n; n->w1o[i] = s->w1[i];
+                        n->p[i] = pn; n->po[i] = s->p[i];
+                        n->w21[i] = w21n;
+                        n->w3[i] = w3n; n->w3o[i] = s->w3[i];
+                        un = w1n + w21n + w3n;
+                    }
+                }
+                if (extra) un += extra[i];
+                n->u[i] = un;
+                n->up[i] = s->u[i];
+            }
+}
+
+int oracle_adj_tlm(const oracle_adj_args *a, const double *fa, const double *fb,
+                   const double *u_hist, const double *extra, double *record)
+{
+    if (!valid(a) || !fa || !fb || !u_hist || !record) return -1;
+    size_t N = (size_t)a->nx * a->ny * a->nz;
+    size_t plane = (size_t)(a->nx - 2 * a->pml) * (a->ny - 2 * a->pml);
+    int prev = omp_get_max_threads();
+    if (a->nthreads > 0) omp_set_num_threads(a->nthreads);
+    dcoef kc;
+    dcoef_init(&kc, a);
+    state s, n;
+    int rc = 0;
+    if (!state_alloc(&s, N) || !state_alloc(&n, N)) {
+        rc = -2;
+        goto out;
+    }
+    for (int k = 0; k < a->nt; k++) {
+        tlm_step(a, &kc, &s, &n, fa + (size_t)k * N, fb + (size_t)k * N, u_hist + (size_t)k * N,
+                 extra ? extra + (size_t)k * N : NULL);
+        swap_state(&s, &n);
+        record_plane(a, s.u, record + (size_t)k * plane);
+    }
+out:
+    state_free(&s);
+    state_free(&n);
+    omp_set_num_threads(prev);
+    return rc;
+}
+
 int oracle_adj_backward(const oracle_adj_args *a, const double *fa, const double *fb,
                         const double *u_hist, const double *resid, double *g_vp,
                         double *g_eps, double *g_del, double *f_adj)

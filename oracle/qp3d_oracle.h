@@ -130,6 +130,12 @@ int oracle_adj_forward(const oracle_adj_args *a, const double *fa, const double 
 int oracle_adj_backward(const oracle_adj_args *a, const double *fa, const double *fb,
                         const double *u_hist, const double *resid, double *g_vp,
                         double *g_eps, double *g_del, double *f_adj);
+/* Tangent-linear run about the base trajectory u_hist (u^k before each step,
+ * nt * N): records (nt * hx * hy) of the response to additive sources extra
+ * (nt * N); with live = 1 the perturbation of S through the unit normal is
+ * included, so that oracle_adj_backward (same live, f_adj) is its transpose. */
+int oracle_adj_tlm(const oracle_adj_args *a, const double *fa, const double *fb,
+                   const double *u_hist, const double *extra, double *record);
 
 #ifdef __cplusplus
 }

