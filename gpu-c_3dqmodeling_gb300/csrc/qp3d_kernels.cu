@@ -1196,8 +1196,11 @@ __device__ __forceinline__ bool step_tile(const CUtensorMap *tm, const PlanePara
                 h2[j] = fmaf(Uy[j], Uy[j], __fmul_rn(Ux[j], Ux[j]));
                 m2[j] = fmaf(Uz[j], Uz[j], h2[j]);
             }
-            if (SPEC && cell_ok[j])
-                mx = fmaxf(mx, fmaxf(fabsf(Ux[j]), fmaxf(fabsf(Uy[j]), fabsf(Uz[j]))));
+            if (SPEC && cell_ok[j]) {   // three-input max: one instruction fewer per cell
+                float t;
+                asm("max.f32 %0, %1, %2, %3;" : "=f"(t) : "f"(mx), "f"(fabsf(Ux[j])), "f"(fabsf(Uy[j])));
+                mx = fmaxf(t, fabsf(Uz[j]));
+            }
             above[j] = m2[j] > T2lo;
             if (!SPEC && p.dec_in && row_ok) above[j] = (p.dec_in[base >> 5] >> (4 * q + j)) & 1u;
             amb[j] = SPEC && cell_ok[j] && above[j] && !(m2[j] > T2hi);
